@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark: GTEPS of single-root top-down BFS on R-MAT scale 25, edge factor
+16 (seed 5, a/b/c/d = .57/.19/.19/.05, deduplicated, symmetrised, uint32 CSC),
+on one GB300.
+
+One step = one BFS from one seeded root (degree > 0), the unit the reference
+times per run (src/run_bfs_gpu.hpp:679-728).  GTEPS = edgesCount / BFS time
+(src/host.cpp:196), edgesCount = sum of out-degrees of expanded vertices.
+
+  value     device time (CUDA events on the engine's stream) of the whole BFS
+            with the graph resident in HBM: level init, every level, no copies
+  e2e       the same metric through the public C call bfs_run with a pinned
+            host output buffer: root in, the n-entry int32 level array copied
+            back inside the timed region, wall clock
+  roofline  the explore kernel (dominant): algorithmic bytes 4*E + 8*F per
+            launch (edges + frontier {beg,end} entries) / its CUDA-event time
+  cpu_baseline  the oracle (C restatement of run_bfs_cpu) on one root of the
+            same graph, one host thread
+
+--impl reference times the reference's CPU BFS (the oracle port of
+run_bfs_cpu; the compiled reference cannot travel to this machine) on every
+host thread: each step runs one single-threaded BFS per thread, distinct roots.
+
+N > 1 (torchrun): replicas only -- every rank runs the same workload on its own
+GPU with its own roots; value = edges of all ranks / max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bfs-gpu-sycl_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "GTEPS at RMAT-25/EF16 on 1xGB300 (single-root top-down BFS)"
+UNIT = "GTEPS"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=25)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--lb", default="llb", help="explore plan for `value`")
+    ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--skip-arms", action="store_true", help="omit the per-arm table")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling in the background (read-only)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+              "utilization.gpu")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.path = os.path.join("/tmp", f"bfs_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 10:
+                continue
+            try:
+                rows.append(dict(sm=float(p[1]), smax=float(p[2]), power=float(p[3]),
+                                 hw=p[5], hwt=p[6], swt=p[7], pcap=p[8],
+                                 util=float(p[9]) if p[9] not in ("", "[N/A]") else 0.0))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        busy = [r for r in rows if r["util"] > 0] or rows
+        reasons = set()
+        for r in busy:
+            for k, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                            ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r[k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in busy),
+                "sm_max_mhz": max(r["smax"] for r in rows),
+                "reasons": sorted(reasons), "samples": len(busy),
+                "power_w_max": max(r["power"] for r in rows)}
+
+
+def dist_setup(backend):
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def reduce_max_sum(vals_max, vals_sum, world):
+    """Max over ranks of vals_max and sum over ranks of vals_sum."""
+    if world == 1:
+        return list(vals_max), list(vals_sum)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    a = torch.tensor(vals_max, dtype=torch.float64, device=dev)
+    b = torch.tensor(vals_sum, dtype=torch.float64, device=dev)
+    dist.all_reduce(a, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return a.cpu().tolist(), b.cpu().tolist()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def bfs_bytes(edges, reached, n):
+    """Algorithmic bytes of one BFS: 4 per traversed edge, 16 per reached
+    vertex (indptr pair, frontier write, frontier read), 4 per vertex (level)."""
+    return 4.0 * edges + 16.0 * reached + 4.0 * n
+
+
+def run_gb300(a):
+    import numpy as np
+    import torch
+    import bfs_gb300 as B
+
+    rank, world, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    hbm_peak, peak_kind = peaks()
+
+    t = time.perf_counter()
+    dg = B.Graph.gen_rmat_device(a.scale, a.edge_factor, seed=a.seed)
+    gen_s = time.perf_counter() - t
+    n = dg.n_cols
+    host = dg.download()
+    roots = B.sample_roots(host, a.warmup + a.steps + 8, a.seed + 1000 * rank)
+    lv = torch.empty(n, dtype=torch.int32, device="cuda")
+    opts = B.options(a.lb, a.block)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    for r in roots[:a.warmup]:
+        dg.run_device(int(r), lv.data_ptr(), opts=opts)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall0 = time.perf_counter()
+    dev_ms, edges, reached, launches = [], [], [], 0
+    for r in roots[a.warmup:a.warmup + a.steps]:
+        st = dg.run_device(int(r), lv.data_ptr(), opts=opts)
+        dev_ms.append(st.device_ms)
+        edges.append(st.edges_count)
+        reached.append(st.reached)
+        launches += st.launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(world)
+    # keep the GPU busy a little longer so the clock record has load samples
+    extra = 0.0
+    while extra < 0.6:
+        t = time.perf_counter()
+        dg.run_device(int(roots[a.warmup]), lv.data_ptr(), opts=opts)
+        extra += time.perf_counter() - t
+    clocks = sampler.stop()
+
+    # correctness spot check of the last timed run (device Graph500 checks)
+    bad = dg.validate_device(int(roots[a.warmup + a.steps - 1]), lv.data_ptr())
+
+    total_ms = sum(dev_ms)
+    tot_edges = float(sum(edges))
+    (max_ms,), (sum_edges,) = reduce_max_sum([total_ms], [tot_edges], world)
+    value = sum_edges / (max_ms * 1e-3) / 1e9
+
+    # e2e through bfs_run: root in, level array out to pinned host memory
+    pinned = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    e2e_steps = max(3, min(a.steps, 10))
+    e_edges, e_wall = 0.0, 0.0
+    for r in roots[:2]:
+        dg.run_into(int(r), pinned.data_ptr(), opts=opts)
+    barrier(world)
+    for r in roots[a.warmup:a.warmup + e2e_steps]:
+        t = time.perf_counter()
+        st = dg.run_into(int(r), pinned.data_ptr(), opts=opts)
+        e_wall += time.perf_counter() - t
+        e_edges += st.edges_count
+    (e_wall_max,), (e_edges_sum,) = reduce_max_sum([e_wall], [e_edges], world)
+    e2e = e_edges_sum / e_wall_max / 1e9
+
+    # explore-kernel roofline: per-level CUDA-event times in the host loop
+    prof_bytes, prof_ms, gen_ms, lvl_rows = 0.0, 0.0, 0.0, []
+    for r in roots[a.warmup:a.warmup + 3]:
+        st = dg.run_device(int(r), lv.data_ptr(),
+                           opts=B.options(a.lb, a.block, loop="host", record=2))
+        tab = st.levels_table()
+        for i in range(st.recorded):
+            F, EF = tab["frontier"][i], tab["edges"][i]
+            if F == 0:
+                continue
+            prof_bytes += 4.0 * EF + 8.0 * F
+            prof_ms += tab["explore_ms"][i]
+            gen_ms += tab["gen_ms"][i]
+            if r == roots[a.warmup]:
+                lvl_rows.append([i, F, EF, round(tab["explore_ms"][i], 4),
+                                 round(tab["gen_ms"][i], 4)])
+    achieved = prof_bytes / (prof_ms * 1e-3) / 1e9 if prof_ms > 0 else None
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "explore_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get("traffic_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # per-arm table (GTEPS of every explore form x block size, graph loop)
+    arms = {}
+    if not a.skip_arms:
+        for lb in ("llb", "glb", "slb"):
+            for blk in (128, 256, 512):
+                o = B.options(lb, blk)
+                dg.run_device(int(roots[0]), lv.data_ptr(), opts=o)
+                ms, ed = 0.0, 0.0
+                for r in roots[a.warmup:a.warmup + 4]:
+                    st = dg.run_device(int(r), lv.data_ptr(), opts=o)
+                    ms += st.device_ms
+                    ed += st.edges_count
+                arms[f"{lb}{blk}"] = round(ed / (ms * 1e-3) / 1e9, 3)
+
+    # CPU baseline: the oracle on one root, one thread (rank 0 only)
+    cpu = None
+    if rank == 0 and not a.skip_cpu:
+        import bfs_oracle as O
+        r = int(roots[a.warmup])
+        t = time.perf_counter()
+        ref, ec = O.oracle_bfs(host.indptr, host.inds, r)
+        cpu_s = time.perf_counter() - t
+        st = dg.run_device(r, lv.data_ptr(), opts=opts)
+        match = bool(np.array_equal(lv.cpu().numpy(), ref)) and st.edges_count == ec
+        cpu = {"value": round(ec / cpu_s / 1e9, 4), "unit": UNIT, "cores": 1,
+               "kind": "port", "sample": f"one BFS from root {r} of the same RMAT-{a.scale} "
+               f"graph, level-synchronous run_bfs_cpu restatement, {cpu_s:.2f} s",
+               "parity_with_gpu": match}
+
+    mean_edges = tot_edges / len(edges)
+    mean_reached = sum(reached) / len(reached)
+    bfs_gbs = bfs_bytes(mean_edges, mean_reached, n) / ((total_ms / len(dev_ms)) * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(total_ms / len(dev_ms), 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded R-MAT generated on the device)",
+        "config": {"workload": f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, single-root "
+                   f"BFS, explore plan {a.lb}{a.block}, device CUDA-graph level loop",
+                   "vertices": n, "edges": dg.nnz, "roots_timed": a.steps,
+                   "l2": "inputs larger than L2 (4 B x edges >> 129 MB)",
+                   "graph_gen_s": round(gen_s, 2), "timed_wall_s": round(wall, 4)},
+        "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": 4,
+                "d2h_bytes_per_step": 4 * n},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                     "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(achieved / hbm_peak, 4) if achieved else None,
+                     "traffic": traffic, "kernel": "explore",
+                     "peak_kind": peak_kind,
+                     "bfs_bytes_per_s_GBs": round(bfs_gbs, 1),
+                     "bfs_frac": round(bfs_gbs / hbm_peak, 4),
+                     "explore_share": round(prof_ms / (prof_ms + gen_ms), 3) if prof_ms else None},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "validator_violations": int(bad),
+        "arms_gteps": arms,
+        "levels_first_root": lvl_rows,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    dg.free()
+
+
+def run_reference(a):
+    """The reference's CPU BFS (oracle port of run_bfs_cpu) on every host
+    thread, same workload; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import bfs_gb300 as B
+    import bfs_oracle as O
+    nthreads = os.cpu_count() or 1
+    t = time.perf_counter()
+    g = B.gen_rmat(a.scale, a.edge_factor, seed=a.seed)
+    gen_s = time.perf_counter() - t
+    roots = B.sample_roots(g, nthreads * (a.warmup + a.steps), a.seed)
+    times, edges = [], []
+    for s in range(a.warmup + a.steps):
+        rs = roots[s * nthreads:(s + 1) * nthreads]
+        t = time.perf_counter()
+        _, ec = O.oracle_bfs_many(g.indptr, g.inds, rs, n_threads=nthreads, keep_levels=False)
+        dt = time.perf_counter() - t
+        if s >= a.warmup:
+            times.append(dt)
+            edges.append(float(ec.sum()))
+    value = sum(edges) / sum(times) / 1e9
+    sample = (f"each step: {nthreads} concurrent single-threaded level-synchronous BFS runs "
+              f"(run_bfs_cpu restatement) from distinct roots of RMAT-{a.scale}/EF{a.edge_factor}")
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+           "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": round(1e3 * sum(times) / len(times), 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+           "data": "synthetic (seeded R-MAT, host generator)",
+           "config": {"workload": f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, "
+                      f"single-root BFS", "vertices": g.n_cols, "edges": g.nnz,
+                      "graph_gen_s": round(gen_s, 2)},
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthreads,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,312 @@
+"""Python binding of the C ABI in include/bfs_gb300.h (ctypes, no torch types).
+
+The library is the product; this module only marshals numpy arrays and raw
+device pointers into the C calls.  It raises if lib/libbfs_gb300.so is
+missing: there is no CPU fallback anywhere in the engine.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libbfs_gb300.so")
+
+LB_LLB, LB_GLB, LB_SLB, LB_LEARNED = 0, 1, 2, 3
+LB_NAMES = {"llb": LB_LLB, "glb": LB_GLB, "slb": LB_SLB, "learned": LB_LEARNED}
+LOOP_GRAPH, LOOP_HOST = 0, 1
+MAX_RECORDED_LEVELS = 4096
+
+STATUS = {
+    0: "BFS_OK", 1: "BFS_ERR_INVALID_ARG", 2: "BFS_ERR_ROOT", 3: "BFS_ERR_GRAPH",
+    4: "BFS_ERR_CUDA", 5: "BFS_ERR_OOM", 6: "BFS_ERR_IO", 7: "BFS_ERR_LEVEL_LIMIT",
+    8: "BFS_ERR_NO_DEVICE", 9: "BFS_ERR_UNSUPPORTED", 10: "BFS_ERR_DEVICE",
+}
+
+
+class BfsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+        self.status = STATUS.get(code, str(code))
+
+
+class Options(C.Structure):
+    _fields_ = [("lb", C.c_int32), ("block", C.c_int32), ("sm_factor", C.c_int32),
+                ("loop", C.c_int32), ("l2_pin", C.c_int32), ("record", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("edges_count", C.c_uint64), ("num_levels", C.c_uint32),
+                ("reached", C.c_uint32), ("device_ms", C.c_double),
+                ("launches", C.c_uint32), ("recorded", C.c_uint32),
+                ("level_frontier", C.c_uint32 * MAX_RECORDED_LEVELS),
+                ("level_edges", C.c_uint32 * MAX_RECORDED_LEVELS),
+                ("level_arm", C.c_int32 * MAX_RECORDED_LEVELS),
+                ("level_explore_ms", C.c_float * MAX_RECORDED_LEVELS),
+                ("level_gen_ms", C.c_float * MAX_RECORDED_LEVELS)]
+
+    def levels_table(self):
+        n = self.recorded
+        return {"frontier": list(self.level_frontier[:n]),
+                "edges": list(self.level_edges[:n]),
+                "arm": list(self.level_arm[:n]),
+                "explore_ms": list(self.level_explore_ms[:n]),
+                "gen_ms": list(self.level_gen_ms[:n])}
+
+
+class CscHost(C.Structure):
+    _fields_ = [("n_rows", C.c_uint32), ("n_cols", C.c_uint32), ("nnz", C.c_uint64),
+                ("indptr", C.POINTER(C.c_uint32)), ("inds", C.POINTER(C.c_uint32))]
+
+
+_lib = None
+U32P = C.POINTER(C.c_uint32)
+I32P = C.POINTER(C.c_int32)
+VP = C.c_void_p
+
+
+def _sig(lib, name, args, res=C.c_int):
+    f = getattr(lib, name)
+    f.argtypes = args
+    f.restype = res
+    return f
+
+
+def lib():
+    """Loads the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} not found: run bfs-gpu-sycl_gb300/build.py first")
+    L = C.CDLL(LIB_PATH)
+    _sig(L, "bfs_abi_version", [])
+    _sig(L, "bfs_status_string", [C.c_int], C.c_char_p)
+    _sig(L, "bfs_last_error", [], C.c_char_p)
+    _sig(L, "bfs_options_default", [C.POINTER(Options)], None)
+    _sig(L, "bfs_graph_upload", [U32P, U32P, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int,
+                                 C.POINTER(VP)])
+    _sig(L, "bfs_graph_wrap_device", [VP, VP, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int,
+                                      C.POINTER(VP)])
+    _sig(L, "bfs_graph_free", [VP])
+    _sig(L, "bfs_graph_info", [VP, U32P, U32P, C.POINTER(C.c_uint64)])
+    _sig(L, "bfs_graph_device_csc", [VP, C.POINTER(VP), C.POINTER(VP)])
+    _sig(L, "bfs_run", [VP, C.c_uint32, C.POINTER(Options), I32P, I32P, C.POINTER(Stats)])
+    _sig(L, "bfs_run_device", [VP, C.c_uint32, C.POINTER(Options), VP, VP, C.POINTER(Stats)])
+    _sig(L, "bfs_validate_device", [VP, C.c_uint32, VP, VP, C.POINTER(C.c_uint64)])
+    _sig(L, "bfs_csc_host_free", [C.POINTER(CscHost)], None)
+    _sig(L, "bfs_gen_rmat_host", [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                  C.c_uint64, C.c_int, C.POINTER(CscHost)])
+    _sig(L, "bfs_gen_rmat_device", [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                    C.c_uint64, C.c_int, C.POINTER(VP)])
+    _sig(L, "bfs_gen_grid_host", [C.c_uint32, C.c_uint32, C.c_double, C.c_uint64,
+                                  C.POINTER(CscHost)])
+    _sig(L, "bfs_gen_er_host", [C.c_uint32, C.c_double, C.c_uint64, C.POINTER(CscHost)])
+    _sig(L, "bfs_graph_download", [VP, C.POINTER(CscHost)])
+    _sig(L, "bfs_sample_roots", [U32P, C.c_uint32, C.c_uint32, C.c_uint64, U32P])
+    _sig(L, "bfs_dataset_load", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost)])
+    _sig(L, "bfs_dataset_write", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost)])
+    _sig(L, "bfs_dataset_read_meta", [C.c_char_p, U32P, U32P, C.POINTER(C.c_uint64), U32P,
+                                      C.c_uint32, U32P])
+    _lib = L
+    return L
+
+
+def check(code):
+    if code != 0:
+        raise BfsError(code, lib().bfs_last_error().decode(errors="replace"))
+
+
+def _u32(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a, a.ctypes.data_as(U32P)
+
+
+class Csc:
+    """Host CSC graph in the reference layout (numpy arrays)."""
+
+    def __init__(self, indptr, inds, n_rows=None, n_cols=None):
+        self.indptr = np.ascontiguousarray(indptr, dtype=np.uint32)
+        self.inds = np.ascontiguousarray(inds, dtype=np.uint32)
+        self.n_cols = int(n_cols if n_cols is not None else len(self.indptr) - 1)
+        self.n_rows = int(n_rows if n_rows is not None else self.n_cols)
+
+    @property
+    def nnz(self):
+        return int(self.inds.shape[0])
+
+    def degree(self):
+        return np.diff(self.indptr.astype(np.int64))
+
+    @staticmethod
+    def _from_c(ch):
+        n = ch.n_cols
+        ip = np.ctypeslib.as_array(ch.indptr, shape=(n + 1,)).copy()
+        ix = (np.ctypeslib.as_array(ch.inds, shape=(ch.nnz,)).copy() if ch.nnz
+              else np.zeros(0, np.uint32))
+        out = Csc(ip, ix, ch.n_rows, ch.n_cols)
+        lib().bfs_csc_host_free(C.byref(ch))
+        return out
+
+    def _to_c(self):
+        ch = CscHost()
+        ch.n_rows, ch.n_cols, ch.nnz = self.n_rows, self.n_cols, self.nnz
+        ch.indptr = self.indptr.ctypes.data_as(U32P)
+        ch.inds = self.inds.ctypes.data_as(U32P)
+        return ch
+
+
+def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetrize=True):
+    ch = CscHost()
+    check(lib().bfs_gen_rmat_host(scale, edge_factor, a, b, c, seed, int(symmetrize),
+                                  C.byref(ch)))
+    return Csc._from_c(ch)
+
+
+def gen_grid(width, height, delete_prob=0.05, seed=3):
+    ch = CscHost()
+    check(lib().bfs_gen_grid_host(width, height, delete_prob, seed, C.byref(ch)))
+    return Csc._from_c(ch)
+
+
+def gen_er(n, avg_degree=16.0, seed=4):
+    ch = CscHost()
+    check(lib().bfs_gen_er_host(n, avg_degree, seed, C.byref(ch)))
+    return Csc._from_c(ch)
+
+
+def sample_roots(g, count, seed):
+    ip, ipp = _u32(g.indptr)
+    out = np.zeros(count, np.uint32)
+    check(lib().bfs_sample_roots(ipp, g.n_rows, count, seed, out.ctypes.data_as(U32P)))
+    return out
+
+
+def dataset_load(name, partitions=1, directory=None):
+    ch = CscHost()
+    check(lib().bfs_dataset_load(directory.encode() if directory else None, name.encode(),
+                                 partitions, C.byref(ch)))
+    return Csc._from_c(ch)
+
+
+def dataset_write(g, name, partitions=1, directory=None):
+    ch = g._to_c()
+    check(lib().bfs_dataset_write(directory.encode() if directory else None, name.encode(),
+                                  partitions, C.byref(ch)))
+
+
+def dataset_read_meta(path, max_records=64):
+    rows = np.zeros(max_records, np.uint32)
+    cols = np.zeros(max_records, np.uint32)
+    nnz = np.zeros(max_records, np.uint64)
+    start = np.zeros(max_records, np.uint32)
+    cnt = C.c_uint32(0)
+    check(lib().bfs_dataset_read_meta(path.encode(), rows.ctypes.data_as(U32P),
+                                      cols.ctypes.data_as(U32P),
+                                      nnz.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                      start.ctypes.data_as(U32P), max_records, C.byref(cnt)))
+    k = min(cnt.value, max_records)
+    return [(int(rows[i]), int(cols[i]), int(nnz[i]), int(start[i])) for i in range(k)]
+
+
+def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=0):
+    o = Options()
+    lib().bfs_options_default(C.byref(o))
+    o.lb = LB_NAMES[lb] if isinstance(lb, str) else int(lb)
+    o.block = int(block)
+    o.sm_factor = int(sm_factor)
+    o.loop = LOOP_GRAPH if loop == "graph" else LOOP_HOST
+    o.l2_pin = int(bool(l2_pin))
+    o.record = int(record)
+    return o
+
+
+class Graph:
+    """A graph resident on the current CUDA device (owns a C handle)."""
+
+    def __init__(self, handle):
+        self.h = VP(handle) if not isinstance(handle, VP) else handle
+        r, c_, z = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        check(lib().bfs_graph_info(self.h, C.byref(r), C.byref(c_), C.byref(z)))
+        self.n_rows, self.n_cols, self.nnz = r.value, c_.value, z.value
+
+    @staticmethod
+    def upload(g, validate=True):
+        ip, ipp = _u32(g.indptr)
+        ix, ixp = _u32(g.inds if g.nnz else np.zeros(1, np.uint32))
+        h = VP()
+        check(lib().bfs_graph_upload(ipp, ixp, g.n_rows, g.n_cols, g.nnz, int(validate),
+                                     C.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def wrap_device(d_indptr, d_inds, n_rows, n_cols, nnz, validate=True):
+        h = VP()
+        check(lib().bfs_graph_wrap_device(VP(d_indptr), VP(d_inds), n_rows, n_cols, nnz,
+                                          int(validate), C.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def gen_rmat_device(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1,
+                        symmetrize=True):
+        h = VP()
+        check(lib().bfs_gen_rmat_device(scale, edge_factor, a, b, c, seed, int(symmetrize),
+                                        C.byref(h)))
+        return Graph(h)
+
+    def download(self):
+        ch = CscHost()
+        check(lib().bfs_graph_download(self.h, C.byref(ch)))
+        return Csc._from_c(ch)
+
+    def device_csc(self):
+        ip, ix = VP(), VP()
+        check(lib().bfs_graph_device_csc(self.h, C.byref(ip), C.byref(ix)))
+        return ip.value, ix.value
+
+    def run(self, root, opts=None, parents=False, stats=True):
+        """One BFS into host arrays; returns (levels, parents or None, Stats)."""
+        lv = np.empty(self.n_cols, np.int32)
+        pa = np.empty(self.n_cols, np.int32) if parents else None
+        st = Stats() if stats else None
+        check(lib().bfs_run(self.h, int(root), C.byref(opts) if opts is not None else None,
+                            lv.ctypes.data_as(I32P),
+                            pa.ctypes.data_as(I32P) if parents else None,
+                            C.byref(st) if st is not None else None))
+        return lv, pa, st
+
+    def run_into(self, root, levels_host_ptr, parents_host_ptr=None, opts=None, stats=True):
+        """One BFS into caller-provided host buffers (e.g. pinned memory)."""
+        st = Stats() if stats else None
+        check(lib().bfs_run(self.h, int(root), C.byref(opts) if opts is not None else None,
+                            C.cast(levels_host_ptr, I32P),
+                            C.cast(parents_host_ptr, I32P) if parents_host_ptr else None,
+                            C.byref(st) if st is not None else None))
+        return st
+
+    def run_device(self, root, levels_ptr, parents_ptr=None, opts=None, stats=True):
+        st = Stats() if stats else None
+        check(lib().bfs_run_device(self.h, int(root),
+                                   C.byref(opts) if opts is not None else None,
+                                   VP(levels_ptr), VP(parents_ptr) if parents_ptr else None,
+                                   C.byref(st) if st is not None else None))
+        return st
+
+    def validate_device(self, root, levels_ptr, parents_ptr=None):
+        bad = C.c_uint64(0)
+        check(lib().bfs_validate_device(self.h, int(root), VP(levels_ptr),
+                                        VP(parents_ptr) if parents_ptr else None,
+                                        C.byref(bad)))
+        return bad.value
+
+    def free(self):
+        if self.h:
+            lib().bfs_graph_free(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

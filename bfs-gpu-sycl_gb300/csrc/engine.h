@@ -1,0 +1,70 @@
+// engine.h -- the graph handle and engine-internal hooks.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <vector>
+
+#include "bfs_internal.h"
+
+namespace bfsgb {
+
+struct GraphEntry {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+struct SchedModel;
+
+// Hooks of the host-driven level loop: `choose` picks the explore arm of a
+// level (learned scheduler, recorder), `before`/`after` bracket the explore
+// launch (per-level timing).  Any of them may be null.
+struct LevelTimer {
+  void *ctx = nullptr;
+  int (*choose)(void *ctx, bfs_graph *g, uint32_t level, uint32_t F, uint32_t EF) = nullptr;
+  void (*before)(void *ctx, bfs_graph *g, uint32_t level, int arm) = nullptr;
+  void (*after)(void *ctx, bfs_graph *g, uint32_t level, int arm) = nullptr;
+};
+
+bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts,
+                           int32_t *levels_dev, int32_t *parents_dev, bfs_stats *stats,
+                           LevelTimer *timer);
+// learned-scheduler level loop (sched.cu)
+bfs_status run_learned(bfs_graph *g, const bfs_options &o, LevelTimer *timer,
+                       uint32_t *launches);
+void free_sched(bfs_graph *g);
+
+}  // namespace bfsgb
+
+struct bfs_graph {
+  int device = 0;
+  int num_sms = 0;
+  uint32_t *indptr = nullptr;
+  uint32_t *inds = nullptr;
+  bool owns_csc = false;
+  uint32_t n_rows = 0, n_cols = 0;
+  uint64_t nnz = 0;
+  uint32_t words = 0;
+  void *ws = nullptr;  // bitmaps, queues, per-level records
+  size_t ws_bytes = 0;
+  size_t bitmap_bytes = 0;
+  bfsgb::BfsDevState tmpl{};  // host template of the device state
+  bfsgb::BfsDevState *d_st = nullptr;
+  bfsgb::BfsDevState *h_st = nullptr;  // pinned mirror
+  int32_t *d_out_levels = nullptr;     // scratch outputs of bfs_run
+  int32_t *d_out_parents = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t lvl_ev[3] = {nullptr, nullptr, nullptr};  // per-level kernel timing
+  float *prof_explore = nullptr;  // host arrays filled by the host loop (record == 2)
+  float *prof_gen = nullptr;
+  int occ[bfsgb::kNumArms] = {};
+  int lg_grid = 0;
+  bool l2_pinned = false;
+  bool use_l2_pin = true;
+  cudaAccessPolicyWindow l2_window{};
+  std::map<int, bfsgb::GraphEntry> graphs;
+  int32_t host_arms[BFS_MAX_RECORDED_LEVELS] = {};
+  uint32_t host_launches = 0;
+  bfsgb::SchedModel *sched = nullptr;
+};

@@ -1,0 +1,590 @@
+// kernels.cu -- sm_103a kernels of the level-synchronous top-down BFS.
+//
+// Per level the reference runs an explore kernel (src/run_bfs_gpu.hpp:388-477
+// for LLB/SLB, :175-385 for GLB) that marks unvisited neighbours of the
+// frontier in byte masks, then a level-generation kernel (:481-521) that scans
+// every vertex, writes levels and appends the new frontier with one atomic per
+// vertex.  The same two-step structure is kept here, redesigned for GB300:
+//
+//   explore   frontier queue entries carry {beg, end} of their edge range, so
+//             the per-level indptr gather moves out of the edge loop.  Edges
+//             are processed in warp rounds of 32 consecutive edges (coalesced
+//             reads of the edge array, streamed with an L2 evict-first policy
+//             and no L1 allocation).  The owner entry of each edge is resolved
+//             with a warp OR-reduction of entry boundaries plus popc instead of
+//             a per-edge binary search (:448-464, :336-346).
+//             Visiting tests one bit of a visited bitmap (n/8 bytes, pinned in
+//             L2 through an access-policy window) with a plain load and only
+//             then claims it with atomicOr, instead of byte masks.
+//   levelgen  scans the bitmap words (n/32, not n bytes): new = vis & ~prev.
+//             Per warp: ballot over the 32 bits of each non-empty word,
+//             popc for positions, one reduction per word for degrees, one
+//             atomic per block for the queue tail.  The atomic adds
+//             (count << 32 | degree sum), so every entry also receives the
+//             exclusive prefix of degrees in queue order: the grid-wide scan
+//             that GLB needs comes out of the same atomic.
+//             Zero-degree vertices and vertices >= n_rows get their level but
+//             are not queued (they would expand nothing; run_bfs_cpu.hpp:31
+//             never expands tid >= numRows).
+//   finish    the last level-generation block swaps the queues, accumulates
+//             edgesCount and, in the CUDA-graph loop, sets the while-node
+//             condition, so no host round trip happens between levels.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "bfs_internal.h"
+#include "kernels.h"
+
+namespace bfsgb {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+// ---- device helpers ---------------------------------------------------------
+
+// Edge-array load: read once per BFS, so bypass L1 and mark evict-first in L2
+// to keep the L2 for the visited bitmaps and queues.
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p, uint64_t pol) {
+  uint32_t r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+               : "=r"(r)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// Test-then-claim of bit n.  The plain load may see a stale 0 (L1 copy);
+// atomicOr's return value is authoritative, so exactly one thread claims n.
+__device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent,
+                                      uint32_t from) {
+  const uint32_t w = n >> 5, bit = 1u << (n & 31u);
+  if (vis[w] & bit) return;
+  const uint32_t old = atomicOr(vis + w, bit);
+  if (parent && !(old & bit)) parent[n] = (int32_t)from;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, uint32_t lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(kFull, x, d);
+    if (lane >= (uint32_t)d) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long x,
+                                                               uint32_t lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long y = __shfl_up_sync(kFull, x, d);
+    if (lane >= (uint32_t)d) x += y;
+  }
+  return x;
+}
+
+// Owner resolution for one warp round.  `cur` is an entry whose start is at
+// or before the round base rb, `bnd` the start offset of entry cur + 1 + lane
+// (all entries have degree >= 1, so starts are distinct).  Returns the entry
+// owning edge rb + lane.
+__device__ __forceinline__ uint32_t round_owner(uint32_t cur, uint32_t bnd,
+                                                uint32_t rb, uint32_t lane) {
+  const uint32_t p = bnd - rb;  // wraps to a large value when bnd < rb
+  const uint32_t bits = (p < 32u) ? (1u << p) : 0u;
+  const uint32_t starts = __reduce_or_sync(kFull, bits);
+  return cur + __popc(starts & ((2u << lane) - 1u));
+}
+
+// ---- fill / init --------------------------------------------------------------
+
+__global__ void fill_kernel(BfsDevState *st) {
+  int32_t *level = st->level, *parent = st->parent;
+  const uint32_t n = st->n_cols;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // int4 stores for the body when both buffers are 16-byte aligned
+  const bool vec = ((reinterpret_cast<uintptr_t>(level) |
+                     reinterpret_cast<uintptr_t>(parent)) & 15u) == 0;
+  const uint32_t n4 = vec ? (n >> 2) : 0u;
+  int4 neg = make_int4(-1, -1, -1, -1);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    reinterpret_cast<int4 *>(level)[i] = neg;
+    if (parent) reinterpret_cast<int4 *>(parent)[i] = neg;
+  }
+  for (uint32_t i = (n4 << 2) + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    level[i] = -1;
+    if (parent) parent[i] = -1;
+  }
+}
+
+__global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t r = st->root;
+  st->vis[r >> 5] |= 1u << (r & 31u);
+  st->prev[r >> 5] |= 1u << (r & 31u);
+  st->level[r] = 0;
+  if (st->parent) st->parent[r] = (int32_t)r;
+  const bool expanded = r < st->n_rows;  // run_bfs_cpu.hpp:31
+  uint32_t b = 0, e = 0;
+  if (expanded) {
+    b = st->indptr[r];
+    e = st->indptr[r + 1];
+  }
+  if (expanded && e > b) {
+    st->qe[0][0] = make_uint2(b, e);
+    st->qp[0][0] = 0;
+    st->qv[0][0] = r;
+    st->F = 1;
+    st->EF = e - b;
+  } else {
+    st->F = 0;
+    st->EF = 0;
+  }
+  st->edges_count = expanded ? (unsigned long long)(e - b) : 0ull;
+  st->cur = 0;
+  st->lvl = 0;
+  st->reached = 1;
+  st->reached_prev = 1;
+  st->max_level = 0;
+  st->next_packed = 0;
+  st->done_blocks = 0;
+  st->error = 0;
+  st->launches = 2;
+  st->arm = st->fixed_arm >= 0 ? st->fixed_arm : 0;
+  if (st->rec_cap > 0) {
+    st->rec_frontier[0] = st->F;
+    st->rec_edges[0] = st->EF;
+    st->rec_arm[0] = -1;
+  }
+  if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
+}
+
+// ---- explore: LLB / SLB -----------------------------------------------------
+// A tile of B frontier entries per block iteration.  LLB takes entries
+// tile*B .. tile*B+B-1; SLB takes tile, tile+T, tile+2T, ... with T the
+// number of tiles, the strided mapping of run_bfs_gpu.hpp:416-420.  A block
+// exclusive scan of the tile's degrees (shared memory) splits the tile's
+// edges evenly over the block's warps (block-local balancing, :437-445).
+template <int B, bool STRIDED>
+__global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restrict__ st) {
+  constexpr int NW = B / 32;
+  __shared__ uint32_t s_off[B + 1];
+  __shared__ uint32_t s_beg[B];
+  __shared__ uint32_t s_vid[B];
+  __shared__ uint32_t s_wsum[NW];
+
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  const uint32_t cur_q = st->cur;
+  const uint2 *__restrict__ qe = st->qe[cur_q];
+  const uint32_t *__restrict__ qv = st->qv[cur_q];
+  const uint32_t *__restrict__ inds = st->inds;
+  uint32_t *vis = st->vis;
+  int32_t *parent = st->parent;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t num_tiles = (F + B - 1) / B;
+  const uint64_t pol = evict_first_policy();
+
+  for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+    const uint32_t slot = STRIDED ? tile + threadIdx.x * num_tiles : tile * B + threadIdx.x;
+    uint32_t beg = 0, deg = 0, vid = 0;
+    if (slot < F) {
+      const uint2 e = qe[slot];
+      beg = e.x;
+      deg = e.y - e.x;
+      if (parent) vid = qv[slot];
+    }
+    const uint32_t incl = warp_incl_scan(deg, lane);
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < (uint32_t)NW ? s_wsum[lane] : 0u;
+      w = warp_incl_scan(w, lane);
+      if (lane < (uint32_t)NW) s_wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t total = s_wsum[NW - 1];
+    s_off[threadIdx.x] = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
+    s_beg[threadIdx.x] = beg;
+    s_vid[threadIdx.x] = vid;
+    if (threadIdx.x == 0) s_off[B] = total;
+    __syncthreads();
+
+    // even split of the tile's edges over the warps, in whole warp rounds
+    const uint64_t per_warp = (((uint64_t)total + NW - 1) / NW + 31u) & ~31ull;
+    const uint64_t w0_64 = (uint64_t)warp * per_warp;
+    if (w0_64 < total) {
+      const uint32_t w0 = (uint32_t)w0_64;
+      const uint32_t w1 = (uint32_t)((w0_64 + per_warp < total) ? w0_64 + per_warp : total);
+      // owner of w0: last entry with s_off <= w0 (broadcast reads)
+      uint32_t lo = 0, hi = B;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_off[mid] <= w0) lo = mid; else hi = mid;
+      }
+      uint32_t cur = lo;
+      for (uint32_t base = w0; base < w1; base += 32u * kUnroll) {
+        uint32_t addr[kUnroll], from[kUnroll];
+        bool act[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+          const uint32_t rb = base + 32u * u;
+          const uint32_t e = rb + lane;
+          const uint32_t j = cur + 1u + lane;
+          const uint32_t bnd = (j <= (uint32_t)B) ? s_off[j] : kFull;
+          const uint32_t o = round_owner(cur, bnd, rb, lane);
+          act[u] = (rb < w1) && (e < w1);
+          addr[u] = 0;
+          from[u] = 0;
+          if (act[u]) {
+            addr[u] = s_beg[o] + (e - s_off[o]);
+            from[u] = s_vid[o];
+          }
+          cur = __shfl_sync(kFull, o, 31);
+          if (cur >= (uint32_t)B) cur = B - 1;  // only reached past w1
+        }
+        uint32_t nb[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) nb[u] = act[u] ? ld_stream(inds + addr[u], pol) : 0u;
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++)
+          if (act[u]) visit(vis, nb[u], parent, from[u]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- explore: GLB -----------------------------------------------------------
+// Edge-balanced: the frontier's edges [0, EF) are cut into equal warp chunks
+// dealt over the whole grid (run_bfs_gpu.hpp:318-366 deals single edges over
+// SMs*SM_FACTOR work-groups).  The grid-wide exclusive scan of degrees is the
+// queue's prefix array written by level generation (EN1-EN3, :203-307).
+// A warp finds the owner of its chunk start with a 32-ary search of the scan
+// (one probe per lane and round), then resolves owners per round like LLB.
+constexpr uint32_t kGlbChunk = kGlbChunkEdges;
+
+__device__ __forceinline__ uint32_t warp_owner_search(const uint32_t *__restrict__ qp,
+                                                      uint32_t F, uint32_t x,
+                                                      uint32_t lane) {
+  uint32_t lo = 0, hi = F;  // qp[lo] <= x < qp[hi] (qp[F] = +inf)
+  while (hi - lo > 32u) {
+    const uint32_t step = (hi - lo + 31u) >> 5;
+    const uint32_t j = lo + lane * step;
+    const uint32_t val = (j < hi) ? qp[j] : kFull;
+    const uint32_t m = __ballot_sync(kFull, val <= x);
+    const uint32_t t = 31u - __clz(m);
+    lo = lo + t * step;
+    hi = min(hi, lo + step);
+  }
+  const uint32_t j = lo + lane;
+  const uint32_t val = (j < hi) ? qp[j] : kFull;
+  const uint32_t m = __ballot_sync(kFull, val <= x);
+  return lo + 31u - __clz(m);
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restrict__ st) {
+  constexpr int NW = B / 32;
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  const uint32_t EF = st->EF;
+  const uint32_t cur_q = st->cur;
+  const uint2 *__restrict__ qe = st->qe[cur_q];
+  const uint32_t *__restrict__ qp = st->qp[cur_q];
+  const uint32_t *__restrict__ qv = st->qv[cur_q];
+  const uint32_t *__restrict__ inds = st->inds;
+  uint32_t *vis = st->vis;
+  int32_t *parent = st->parent;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint64_t pol = evict_first_policy();
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + kGlbChunk - 1) / kGlbChunk);
+  const uint32_t total_warps = gridDim.x * NW;
+
+  for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
+    const uint32_t w0 = c * kGlbChunk;
+    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + kGlbChunk);
+    uint32_t cur = warp_owner_search(qp, F, w0, lane);
+    for (uint32_t base = w0; base < w1; base += 32u * kUnroll) {
+      uint32_t addr[kUnroll], from[kUnroll];
+      bool act[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) {
+        const uint32_t rb = base + 32u * u;
+        const uint32_t e = rb + lane;
+        const uint32_t j = cur + 1u + lane;
+        const uint32_t bnd = (j < F) ? qp[j] : (j == F ? EF : kFull);
+        const uint32_t o = round_owner(cur, bnd, rb, lane);
+        act[u] = (rb < w1) && (e < w1);
+        addr[u] = 0;
+        from[u] = 0;
+        if (act[u]) {
+          addr[u] = qe[o].x + (e - qp[o]);
+          if (parent) from[u] = qv[o];
+        }
+        cur = __shfl_sync(kFull, o, 31);
+        if (cur >= F) cur = F - 1;  // only reached past w1
+      }
+      uint32_t nb[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) nb[u] = act[u] ? ld_stream(inds + addr[u], pol) : 0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++)
+        if (act[u]) visit(vis, nb[u], parent, from[u]);
+    }
+  }
+}
+
+// ---- level generation -----------------------------------------------------
+__device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_cond) {
+  const unsigned long long packed = *(volatile unsigned long long *)&st->next_packed;
+  const uint32_t f_new = (uint32_t)(packed >> 32);
+  const uint32_t ef_new = (uint32_t)packed;
+  const uint32_t lvl = st->lvl + 1;
+  const uint32_t reached = *(volatile uint32_t *)&st->reached;
+  if (reached > st->reached_prev) st->max_level = lvl;
+  st->reached_prev = reached;
+  st->edges_count += ef_new;
+  st->cur ^= 1u;
+  st->F = f_new;
+  st->EF = ef_new;
+  st->lvl = lvl;
+  st->next_packed = 0;
+  st->done_blocks = 0;
+  st->launches += 2;
+  if (lvl < st->rec_cap) {
+    st->rec_frontier[lvl] = f_new;
+    st->rec_edges[lvl] = ef_new;
+    st->rec_arm[lvl] = -1;
+  }
+  if (f_new > 0 && lvl >= st->level_cap) {
+    st->error |= BFS_DEVERR_LEVEL_LIMIT;
+    st->F = 0;
+  }
+  if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ st,
+                                                     unsigned long long cond,
+                                                     int use_cond) {
+  constexpr int NW = B / 32;
+  __shared__ unsigned long long s_wtot[NW];
+  __shared__ unsigned long long s_base;
+  __shared__ uint32_t s_reached[NW];
+  __shared__ int s_last;
+
+  const uint32_t words = st->words;
+  uint32_t *__restrict__ V = st->vis;
+  uint32_t *__restrict__ P = st->prev;
+  const uint32_t *__restrict__ indptr = st->indptr;
+  const uint32_t n_rows = st->n_rows;
+  const int32_t lvl_next = (int32_t)st->lvl + 1;
+  int32_t *__restrict__ level = st->level;
+  const uint32_t nq = st->cur ^ 1u;
+  uint2 *__restrict__ qe = st->qe[nq];
+  uint32_t *__restrict__ qp = st->qp[nq];
+  uint32_t *__restrict__ qv = st->qv[nq];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t reached = 0;
+
+  for (uint32_t sb = blockIdx.x * (NW * 32u); sb < words; sb += gridDim.x * (NW * 32u)) {
+    const uint32_t gw = sb + warp * 32u;  // first of this warp's 32 words
+    const uint32_t w = gw + lane;
+    uint32_t newb = 0;
+    if (gw < words) {
+      const uint32_t vw = V[w], pw = P[w];
+      newb = vw & ~pw;
+      if (newb) P[w] = vw;
+    }
+    reached += __popc(newb);
+    const uint32_t nz = __ballot_sync(kFull, newb != 0u);
+    // pass 1: levels, kept entries and their degrees per word
+    unsigned long long mine = 0;  // (count << 32 | degree sum) of word `lane`
+    for (uint32_t m = nz; m; m &= m - 1u) {
+      const uint32_t src = __ffs(m) - 1u;
+      const uint32_t wb = __shfl_sync(kFull, newb, src);
+      const uint32_t v = (gw + src) * 32u + lane;
+      uint32_t deg = 0;
+      if ((wb >> lane) & 1u) {
+        level[v] = lvl_next;
+        if (v < n_rows) deg = indptr[v + 1] - indptr[v];
+      }
+      const uint32_t km = __ballot_sync(kFull, deg > 0u);
+      const uint32_t ds = __reduce_add_sync(kFull, deg);
+      if (lane == src) mine = ((unsigned long long)__popc(km) << 32) | ds;
+    }
+    // block-wide offsets: warp scan, then one atomic per block
+    const unsigned long long incl = warp_incl_scan64(mine, lane);
+    if (lane == 31) s_wtot[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long run = 0;
+      for (int i = 0; i < NW; i++) {
+        const unsigned long long t = s_wtot[i];
+        s_wtot[i] = run;
+        run += t;
+      }
+      s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
+    }
+    __syncthreads();
+    if (nz) {
+      const unsigned long long my_base = s_base + s_wtot[warp] + (incl - mine);
+      // pass 2: write the kept entries
+      for (uint32_t m = nz; m; m &= m - 1u) {
+        const uint32_t src = __ffs(m) - 1u;
+        const uint32_t wb = __shfl_sync(kFull, newb, src);
+        const unsigned long long wbase = __shfl_sync(kFull, my_base, src);
+        const uint32_t v = (gw + src) * 32u + lane;
+        uint32_t b = 0, e = 0;
+        if (((wb >> lane) & 1u) && v < n_rows) {
+          b = indptr[v];
+          e = indptr[v + 1];
+        }
+        const uint32_t deg = e - b;
+        const uint32_t km = __ballot_sync(kFull, deg > 0u);
+        const uint32_t dx = warp_incl_scan(deg, lane) - deg;
+        if (deg) {
+          const uint32_t slot = (uint32_t)(wbase >> 32) + __popc(km & lt_mask);
+          qe[slot] = make_uint2(b, e);
+          qp[slot] = (uint32_t)wbase + dx;
+          qv[slot] = v;
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // reached-vertex count: one atomic per block
+  reached = __reduce_add_sync(kFull, reached);
+  if (lane == 0) s_reached[warp] = reached;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < NW; i++) t += s_reached[i];
+    if (t) atomicAdd(&st->reached, t);
+    __threadfence();
+    const uint32_t ticket = atomicAdd(&st->done_blocks, 1u);
+    s_last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    finish_level(st, cond, use_cond);
+  }
+}
+
+// ---- validation (Graph500-style checks of a level array) --------------------
+// Edge pass: for every expanded reached u and edge u->v: level[v] must be
+// reached and <= level[u] + 1; v gets a witness if level[v] == level[u] + 1,
+// and its parent is confirmed if parent[v] == u.
+__global__ void validate_edges_kernel(const uint32_t *__restrict__ indptr,
+                                      const uint32_t *__restrict__ inds, uint32_t n_rows,
+                                      const int32_t *__restrict__ level,
+                                      const int32_t *__restrict__ parent,
+                                      uint8_t *witness, uint8_t *parent_ok,
+                                      unsigned long long *bad) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long nbad = 0;
+  for (uint32_t u = gwarp; u < n_rows; u += nwarps) {
+    const int32_t lu = level[u];
+    if (lu < 0) continue;
+    const uint32_t b = indptr[u], e = indptr[u + 1];
+    for (uint32_t k = b + lane; k < e; k += 32u) {
+      const uint32_t v = inds[k];
+      const int32_t lv = level[v];
+      if (lv < 0 || lv > lu + 1) nbad++;
+      if (lv == lu + 1) {
+        witness[v] = 1;
+        if (parent && parent[v] == (int32_t)u) parent_ok[v] = 1;
+      }
+    }
+  }
+  nbad = __reduce_add_sync(kFull, (uint32_t)nbad);
+  if (lane == 0 && nbad) atomicAdd(bad, nbad);
+}
+
+// Vertex pass: root at level 0 (and its own parent); any other reached vertex
+// needs a witness in-edge and, with parents, a confirmed parent.
+__global__ void validate_vertices_kernel(uint32_t n_cols, uint32_t root,
+                                         const int32_t *__restrict__ level,
+                                         const int32_t *__restrict__ parent,
+                                         const uint8_t *witness, const uint8_t *parent_ok,
+                                         unsigned long long *bad) {
+  uint32_t nbad = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n_cols;
+       v += gridDim.x * blockDim.x) {
+    const int32_t lv = level[v];
+    if (v == root) {
+      if (lv != 0) nbad++;
+      if (parent && parent[v] != (int32_t)root) nbad++;
+      continue;
+    }
+    if (lv == 0) nbad++;
+    if (lv > 0 && !witness[v]) nbad++;
+    if (parent) {
+      if (lv > 0 && !parent_ok[v]) nbad++;
+      if (lv < 0 && parent[v] != -1) nbad++;
+    }
+  }
+  nbad = __reduce_add_sync(kFull, nbad);
+  if ((threadIdx.x & 31u) == 0 && nbad) atomicAdd(bad, (unsigned long long)nbad);
+}
+
+// CSC check used at upload: indptr monotone, indptr[0] == 0, last == nnz,
+// every destination < n_cols.
+__global__ void check_csc_kernel(const uint32_t *__restrict__ indptr,
+                                 const uint32_t *__restrict__ inds, uint32_t n_cols,
+                                 uint64_t nnz, unsigned long long *bad) {
+  uint32_t nbad = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint64_t v = tid; v < n_cols; v += stride)
+    if (indptr[v + 1] < indptr[v]) nbad++;
+  if (tid == 0 && (indptr[0] != 0 || (uint64_t)indptr[n_cols] != nnz)) nbad++;
+  for (uint64_t k = tid; k < nnz; k += stride)
+    if (inds[k] >= n_cols) nbad++;
+  nbad = __reduce_add_sync(kFull, nbad);
+  if ((threadIdx.x & 31u) == 0 && nbad) atomicAdd(bad, (unsigned long long)nbad);
+}
+
+// ---- kernel table ---------------------------------------------------------
+const void *explore_kernel_fn(int arm) {
+  switch (arm) {
+    case 0: return (const void *)explore_local_kernel<128, false>;
+    case 1: return (const void *)explore_local_kernel<256, false>;
+    case 2: return (const void *)explore_local_kernel<512, false>;
+    case 3: return (const void *)explore_global_kernel<128>;
+    case 4: return (const void *)explore_global_kernel<256>;
+    case 5: return (const void *)explore_global_kernel<512>;
+    case 6: return (const void *)explore_local_kernel<128, true>;
+    case 7: return (const void *)explore_local_kernel<256, true>;
+    case 8: return (const void *)explore_local_kernel<512, true>;
+    default: return nullptr;
+  }
+}
+const void *levelgen_kernel_fn() { return (const void *)levelgen_kernel<kLevelgenBlock>; }
+const void *init_kernel_fn() { return (const void *)init_kernel; }
+const void *fill_kernel_fn() { return (const void *)fill_kernel; }
+
+cudaError_t launch_validate(const uint32_t *indptr, const uint32_t *inds, uint32_t n_rows,
+                            uint32_t n_cols, uint32_t root, const int32_t *level,
+                            const int32_t *parent, uint8_t *witness, uint8_t *parent_ok,
+                            unsigned long long *bad, cudaStream_t s) {
+  validate_edges_kernel<<<2048, 256, 0, s>>>(indptr, inds, n_rows, level, parent, witness,
+                                             parent_ok, bad);
+  validate_vertices_kernel<<<1024, 256, 0, s>>>(n_cols, root, level, parent, witness,
+                                                parent_ok, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_csc(const uint32_t *indptr, const uint32_t *inds, uint32_t n_cols,
+                             uint64_t nnz, unsigned long long *bad, cudaStream_t s) {
+  check_csc_kernel<<<2048, 256, 0, s>>>(indptr, inds, n_cols, nnz, bad);
+  return cudaGetLastError();
+}
+
+}  // namespace bfsgb

@@ -1,0 +1,210 @@
+/*
+ * bfs_gb300.h -- C ABI of the GB300 (sm_103a) breadth-first-search engine.
+ *
+ * This is the drop-in boundary for the reference's single-partition GPU path.
+ * The reference has no FFI: its boundary is the header-only C++ template
+ *   GPURun(vertexCount, IndexHost, OffsetHost, h_visit_mask, h_visit,
+ *          h_distance, sourceNode, num_runs, json, h_visit_offsets)
+ * (src/run_bfs_gpu.hpp:534-542), called from src/host.cpp:149.  The entry
+ * points below split that template into "upload the graph once" and "run one
+ * BFS", with plain pointers and sizes, integer status codes and caller-owned
+ * output buffers.  include/bfs_gpurun.hpp rebuilds the GPURun template on top
+ * of them.
+ *
+ * Conventions
+ *   - Graphs use the reference's single-partition CSC layout
+ *     (src/graph_load.hpp:7-20, scripts/generator.py:115-185): `indptr` has
+ *     n_cols + 1 uint32 offsets, `inds` has nnz uint32 destination ids.  The
+ *     out-neighbours of vertex v are inds[indptr[v] .. indptr[v+1]).
+ *   - Only vertices v < n_rows are expanded (n_rows <= n_cols), exactly as the
+ *     reference's run_bfs_cpu loops tid < numRows (src/run_bfs_cpu.hpp:31).
+ *   - Level arrays are int32[n_cols]: 0 at the root, -1 for unreached
+ *     vertices, otherwise the hop distance (src/host.cpp:113-115).
+ *   - No function throws; every one returns a bfs_status.  bfs_last_error()
+ *     gives a message for the most recent failure on the calling thread.
+ *   - Each graph handle owns one CUDA stream; calls on one handle must not
+ *     overlap from several host threads.
+ */
+#ifndef BFS_GB300_H
+#define BFS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BFS_GB300_ABI_VERSION 1
+
+typedef enum bfs_status {
+  BFS_OK = 0,
+  BFS_ERR_INVALID_ARG = 1,   /* null pointer, bad size or option */
+  BFS_ERR_ROOT = 2,          /* root >= n_cols */
+  BFS_ERR_GRAPH = 3,         /* malformed CSC: indptr not monotone, inds >= n_cols */
+  BFS_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+  BFS_ERR_OOM = 5,           /* device or host allocation failed */
+  BFS_ERR_IO = 6,            /* dataset file missing, empty or truncated */
+  BFS_ERR_LEVEL_LIMIT = 7,   /* device level loop exceeded n_cols + 1 levels */
+  BFS_ERR_NO_DEVICE = 8,     /* no CUDA device visible */
+  BFS_ERR_UNSUPPORTED = 9,   /* option not supported for this graph */
+  BFS_ERR_DEVICE = 10        /* a kernel reported an internal error flag */
+} bfs_status;
+
+/* Load-balancing form of the explore step (the reference picks one at compile
+ * time with USE_GLOBAL_LOAD_BALANCE / USE_STRIDED_LOCAL_LOAD_BALANCE,
+ * src/CMakeLists.txt:10-11). */
+typedef enum bfs_lb {
+  BFS_LB_LLB = 0,      /* local: block-level scan over a tile of the frontier */
+  BFS_LB_GLB = 1,      /* global: grid-wide scan, edges dealt evenly to blocks */
+  BFS_LB_SLB = 2,      /* strided local: frontier dealt round-robin to blocks */
+  BFS_LB_LEARNED = 3   /* per-level choice by the learned scheduler */
+} bfs_lb;
+
+/* How the level loop is driven. */
+typedef enum bfs_loop {
+  BFS_LOOP_GRAPH = 0,  /* CUDA graph with a device-side while loop (default) */
+  BFS_LOOP_HOST = 1    /* host loop, one frontier-size read-back per level,
+                          like src/run_bfs_gpu.hpp:682-727 */
+} bfs_loop;
+
+typedef struct bfs_options {
+  int32_t lb;          /* bfs_lb */
+  int32_t block;       /* threads per block: 128, 256 or 512 (0 = 256) */
+  int32_t sm_factor;   /* blocks per SM for the persistent grid (0 = auto) */
+  int32_t loop;        /* bfs_loop */
+  int32_t l2_pin;      /* 1 = pin the visited bitmaps in L2 (default on) */
+  int32_t record;      /* 1 = fill bfs_stats per-level arrays; 2 = also time
+                          every kernel with CUDA events (forces the host loop) */
+} bfs_options;
+
+#define BFS_MAX_RECORDED_LEVELS 4096
+
+typedef struct bfs_stats {
+  uint64_t edges_count;   /* sum of out-degrees of expanded vertices; the
+                             reference's json["edgesCount"] (run_bfs_cpu.hpp:36,84) */
+  uint32_t num_levels;    /* levels with a non-empty frontier (max level + 1) */
+  uint32_t reached;       /* vertices with level >= 0 */
+  double device_ms;       /* seeded-root to last-level time, CUDA events */
+  uint32_t launches;      /* kernels this engine launched for the run */
+  uint32_t recorded;      /* entries filled in the arrays below */
+  uint32_t level_frontier[BFS_MAX_RECORDED_LEVELS];  /* vertices expanded */
+  uint32_t level_edges[BFS_MAX_RECORDED_LEVELS];     /* edges explored */
+  int32_t level_arm[BFS_MAX_RECORDED_LEVELS];        /* lb*3 + block index */
+  float level_explore_ms[BFS_MAX_RECORDED_LEVELS];   /* record == 2 only */
+  float level_gen_ms[BFS_MAX_RECORDED_LEVELS];       /* record == 2 only */
+} bfs_stats;
+
+typedef struct bfs_graph bfs_graph;
+
+/* ---- library ---------------------------------------------------------- */
+int bfs_abi_version(void);
+const char *bfs_status_string(bfs_status s);
+const char *bfs_last_error(void);
+/* Fills o with the defaults (LLB, 256 threads, graph loop, L2 pin on). */
+void bfs_options_default(bfs_options *o);
+
+/* ---- graph lifetime --------------------------------------------------- */
+/* Copies a host CSC graph to the current CUDA device once (the reference
+ * re-uploads it for every run, src/run_bfs_gpu.hpp:620-670).  validate = 1
+ * checks monotone indptr and inds < n_cols on the device first. */
+bfs_status bfs_graph_upload(const uint32_t *indptr, const uint32_t *inds,
+                            uint32_t n_rows, uint32_t n_cols, uint64_t nnz,
+                            int validate, bfs_graph **out);
+/* Wraps a CSC graph already in device memory (not copied, not freed by
+ * bfs_graph_free; must outlive the handle). */
+bfs_status bfs_graph_wrap_device(const uint32_t *d_indptr, const uint32_t *d_inds,
+                                 uint32_t n_rows, uint32_t n_cols, uint64_t nnz,
+                                 int validate, bfs_graph **out);
+bfs_status bfs_graph_free(bfs_graph *g);
+bfs_status bfs_graph_info(const bfs_graph *g, uint32_t *n_rows, uint32_t *n_cols,
+                          uint64_t *nnz);
+/* Device pointers of the graph's CSC arrays (for callers that gather their
+ * own statistics on the device). */
+bfs_status bfs_graph_device_csc(const bfs_graph *g, const uint32_t **d_indptr,
+                                const uint32_t **d_inds);
+
+/* ---- single-root BFS -------------------------------------------------- */
+/* One BFS from root.  levels_host (n_cols int32, required) and parents_host
+ * (n_cols int32, optional: parent of each reached vertex, the root is its own
+ * parent, -1 if unreached) are host buffers; the device-to-host copy is part
+ * of the call.  stats may be NULL.  opts may be NULL (defaults). */
+bfs_status bfs_run(bfs_graph *g, uint32_t root, const bfs_options *opts,
+                   int32_t *levels_host, int32_t *parents_host, bfs_stats *stats);
+/* Same, with device output buffers (levels_dev required, parents_dev
+ * optional); nothing is copied to the host except the small stats. */
+bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,
+                          int32_t *levels_dev, int32_t *parents_dev,
+                          bfs_stats *stats);
+/* Graph-validation helper (Graph500-style): checks on the device that
+ * levels_dev is the exact BFS level array of root (root at 0, every edge
+ * u->v from an expanded vertex has level[v] <= level[u] + 1, every reached
+ * non-root vertex has an in-edge from level - 1) and, if parents_dev is not
+ * NULL, that every parent is a level-1 in-neighbour.  *bad receives the
+ * number of violations (0 = valid). */
+bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,
+                               const int32_t *parents_dev, uint64_t *bad);
+
+/* ---- synthetic graphs and roots --------------------------------------- */
+/* Seeded generators.  Every edge is a pure function of (seed, index) through
+ * a counter-based hash, so the host and device builders produce identical
+ * graphs.  Self-loops and duplicates are removed; symmetrize = 1 adds the
+ * reverse of every edge.  Output CSC has n_rows == n_cols. */
+typedef struct bfs_csc_host {
+  uint32_t n_rows, n_cols;
+  uint64_t nnz;
+  uint32_t *indptr;   /* n_cols + 1, malloc'ed by the library */
+  uint32_t *inds;     /* nnz, malloc'ed by the library */
+} bfs_csc_host;
+void bfs_csc_host_free(bfs_csc_host *g);
+
+/* R-MAT (a, b, c; d = 1 - a - b - c) with 2^scale vertices and
+ * edge_factor * 2^scale generated edges. */
+bfs_status bfs_gen_rmat_host(uint32_t scale, uint32_t edge_factor, double a,
+                             double b, double c, uint64_t seed, int symmetrize,
+                             bfs_csc_host *out);
+/* Same graph built on the current device and kept there as an engine handle
+ * (no host copy); used for graphs too large to build quickly on the host. */
+bfs_status bfs_gen_rmat_device(uint32_t scale, uint32_t edge_factor, double a,
+                               double b, double c, uint64_t seed, int symmetrize,
+                               bfs_graph **out);
+/* width x height 4-neighbour grid; each undirected edge is deleted with
+ * probability delete_prob. */
+bfs_status bfs_gen_grid_host(uint32_t width, uint32_t height, double delete_prob,
+                             uint64_t seed, bfs_csc_host *out);
+/* Erdos-Renyi style graph: n vertices, n * avg_degree / 2 uniform random
+ * undirected pairs before de-duplication. */
+bfs_status bfs_gen_er_host(uint32_t n, double avg_degree, uint64_t seed,
+                           bfs_csc_host *out);
+/* Copies a device-built graph back to the host (for oracle checks). */
+bfs_status bfs_graph_download(const bfs_graph *g, bfs_csc_host *out);
+/* Draws count distinct roots with out-degree > 0 among vertices < n_rows,
+ * seeded.  Fails with BFS_ERR_GRAPH if fewer than count such vertices exist. */
+bfs_status bfs_sample_roots(const uint32_t *indptr, uint32_t n_rows, uint32_t count,
+                            uint64_t seed, uint32_t *roots_out);
+
+/* ---- reference dataset files ------------------------------------------ */
+/* Reads <dir>/<name>-csc-<P>/<name>-csc-meta.bin plus the partition files,
+ * the layout of src/graph_load.hpp:93-132 (P > 1 partitions are merged into
+ * one CSC in partition order, which gives the same BFS levels and edge
+ * counts as the reference's multi-partition CPU BFS).  dir == NULL means
+ * "$PWD/dataset".  n_rows is the sum of partition rows and n_cols the first
+ * record's cols, as src/host.cpp:86-92 derives them. */
+bfs_status bfs_dataset_load(const char *dir, const char *name, uint32_t partitions,
+                            bfs_csc_host *out);
+/* Writes a single- or multi-partition dataset in the same layout (the
+ * inverse of the above; nnz-balanced row split for P > 1 like
+ * scripts/generator.py:22-40, without its round-to-8 of the breaks). */
+bfs_status bfs_dataset_write(const char *dir, const char *name, uint32_t partitions,
+                             const bfs_csc_host *g);
+/* Reads only the meta records (20 bytes each: u32 rows, u32 cols, u64 nnz,
+ * u32 startRow; src/graph_load.hpp:49-92).  Returns the record count in
+ * *count (at most max_records are stored). */
+bfs_status bfs_dataset_read_meta(const char *meta_path, uint32_t *rows, uint32_t *cols,
+                                 uint64_t *nnz, uint32_t *start_row,
+                                 uint32_t max_records, uint32_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BFS_GB300_H */

@@ -33,7 +33,8 @@ class BfsError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("lb", C.c_int32), ("block", C.c_int32), ("sm_factor", C.c_int32),
-                ("loop", C.c_int32), ("l2_pin", C.c_int32), ("record", C.c_int32)]
+                ("loop", C.c_int32), ("l2_pin", C.c_int32), ("record", C.c_int32),
+                ("ipt", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -53,6 +54,19 @@ class Stats(C.Structure):
                 "arm": list(self.level_arm[:n]),
                 "explore_ms": list(self.level_explore_ms[:n]),
                 "gen_ms": list(self.level_gen_ms[:n])}
+
+
+SCHED_INPUTS, SCHED_ARMS, SCHED_PARAMS = 5, 9, 1545
+ARM_NAMES = [f"{lb}{blk}" for lb in ("llb", "glb", "slb") for blk in (128, 256, 512)]
+
+
+class LevelSample(C.Structure):
+    _fields_ = [("features", C.c_float * SCHED_INPUTS), ("arm_ms", C.c_float * SCHED_ARMS),
+                ("level", C.c_uint32), ("frontier", C.c_uint32), ("edges", C.c_uint32)]
+
+
+class TrainOpts(C.Structure):
+    _fields_ = [("epochs", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64)]
 
 
 class CscHost(C.Structure):
@@ -109,6 +123,13 @@ def lib():
     _sig(L, "bfs_dataset_write", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost)])
     _sig(L, "bfs_dataset_read_meta", [C.c_char_p, U32P, U32P, C.POINTER(C.c_uint64), U32P,
                                       C.c_uint32, U32P])
+    _sig(L, "bfs_sched_record", [VP, C.c_uint32, C.c_int32, C.c_int32, C.POINTER(LevelSample),
+                                 C.c_uint32, U32P])
+    _sig(L, "bfs_sched_train", [C.POINTER(LevelSample), C.c_uint32, C.POINTER(TrainOpts),
+                                C.POINTER(C.c_float), C.POINTER(C.c_float)])
+    _sig(L, "bfs_sched_predict", [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32, I32P,
+                                  C.POINTER(C.c_float)])
+    _sig(L, "bfs_sched_attach", [VP, C.POINTER(C.c_float), C.c_float])
     _lib = L
     return L
 
@@ -210,7 +231,52 @@ def dataset_read_meta(path, max_records=64):
     return [(int(rows[i]), int(cols[i]), int(nnz[i]), int(start[i])) for i in range(k)]
 
 
-def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=0):
+def samples_to_arrays(samples):
+    """LevelSample array -> (features float32[n,5], arm_ms float32[n,9], meta uint32[n,3])."""
+    n = len(samples)
+    f = np.array([list(x.features) for x in samples], np.float32).reshape(n, SCHED_INPUTS)
+    t = np.array([list(x.arm_ms) for x in samples], np.float32).reshape(n, SCHED_ARMS)
+    m = np.array([[x.level, x.frontier, x.edges] for x in samples], np.uint32).reshape(n, 3)
+    return f, t, m
+
+
+def arrays_to_samples(features, arm_ms, meta=None):
+    n = len(features)
+    arr = (LevelSample * n)()
+    for i in range(n):
+        for j in range(SCHED_INPUTS):
+            arr[i].features[j] = float(features[i][j])
+        for j in range(SCHED_ARMS):
+            arr[i].arm_ms[j] = float(arm_ms[i][j])
+        if meta is not None:
+            arr[i].level, arr[i].frontier, arr[i].edges = (int(x) for x in meta[i])
+    return arr
+
+
+def sched_train(features, arm_ms, epochs=1500, lr=3e-3, seed=1):
+    """Trains the scheduler MLP on the device; returns (weights float32[1545], loss)."""
+    samples = arrays_to_samples(features, arm_ms)
+    w = np.zeros(SCHED_PARAMS, np.float32)
+    loss = C.c_float(0)
+    o = TrainOpts(epochs, lr, seed)
+    check(lib().bfs_sched_train(samples, len(samples), C.byref(o),
+                                w.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
+    return w, loss.value
+
+
+def sched_predict(weights, features):
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(features, np.float32).reshape(-1, SCHED_INPUTS)
+    arms = np.zeros(len(x), np.int32)
+    conf = np.zeros(len(x), np.float32)
+    check(lib().bfs_sched_predict(w.ctypes.data_as(C.POINTER(C.c_float)),
+                                  x.ctypes.data_as(C.POINTER(C.c_float)), len(x),
+                                  arms.ctypes.data_as(I32P),
+                                  conf.ctypes.data_as(C.POINTER(C.c_float))))
+    return arms, conf
+
+
+def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=0, ipt=4):
     o = Options()
     lib().bfs_options_default(C.byref(o))
     o.lb = LB_NAMES[lb] if isinstance(lb, str) else int(lb)
@@ -219,6 +285,7 @@ def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=
     o.loop = LOOP_GRAPH if loop == "graph" else LOOP_HOST
     o.l2_pin = int(bool(l2_pin))
     o.record = int(record)
+    o.ipt = int(ipt)
     return o
 
 
@@ -292,6 +359,22 @@ class Graph:
                                    VP(levels_ptr), VP(parents_ptr) if parents_ptr else None,
                                    C.byref(st) if st is not None else None))
         return st
+
+    def sched_record(self, root, ipt=4, reps=3, max_levels=1 << 16):
+        """Per-level features and explore times of all 9 arms for one BFS."""
+        buf = (LevelSample * max_levels)()
+        n = C.c_uint32(0)
+        check(lib().bfs_sched_record(self.h, int(root), ipt, reps, buf, max_levels, C.byref(n)))
+        return buf[:n.value]
+
+    def sched_attach(self, weights, min_confidence=0.0):
+        if weights is None:
+            check(lib().bfs_sched_attach(self.h, None, 0.0))
+            return
+        w = np.ascontiguousarray(weights, np.float32)
+        assert w.size == SCHED_PARAMS
+        check(lib().bfs_sched_attach(self.h, w.ctypes.data_as(C.POINTER(C.c_float)),
+                                     float(min_confidence)))
 
     def validate_device(self, root, levels_ptr, parents_ptr=None):
         bad = C.c_uint64(0)

@@ -5,8 +5,9 @@
 //   inds    u32[nnz]          destination ids
 //   vis     u32[words]        visited bitmap, bit v = vertex v reached
 //   prev    u32[words]        visited bitmap as of the previous level
-//   qe[2]   uint2[n_rows]     frontier queue: {beg, end} of each entry's edges
-//   qp[2]   u32[n_rows]       exclusive prefix of entry degrees (queue order)
+//   qb[2]   u32[n_rows]       frontier queue: first edge (indptr[v]) of each entry
+//   qp[2]   u32[n_rows + 1]   exclusive prefix of entry degrees (queue order);
+//                             qp[F] holds the frontier's edge total
 //   qv[2]   u32[n_rows]       vertex id of each entry
 //   state   BfsDevState       counters of the level loop (one struct)
 // words = ceil(n_cols / 32) rounded up to a multiple of 32 (one warp reads
@@ -18,7 +19,7 @@
 
 #include <vector_types.h>
 
-#include "../../include/bfs_gb300.h"
+#include "bfs_gb300.h"
 
 #if defined(__CUDACC__)
 #define BFS_HD __host__ __device__ __forceinline__
@@ -86,7 +87,7 @@ struct BfsDevState {
   // workspace
   uint32_t *vis;
   uint32_t *prev;
-  uint2 *qe[2];
+  uint32_t *qb[2];
   uint32_t *qp[2];
   uint32_t *qv[2];
   int32_t *level;

@@ -23,6 +23,7 @@
 #include "bfs_internal.h"
 #include "engine.h"
 #include "kernels.h"
+#include "bfs_sched.h"
 
 namespace bfsgb {
 
@@ -101,9 +102,9 @@ static bfs_status setup_workspace(bfs_graph *g) {
   // one allocation: bitmaps (vis, prev), three queue arrays x 2, record arrays
   const size_t bm = align_up((size_t)g->words * 4, 256);
   const size_t nq = std::max<size_t>(g->n_rows, 1);
-  const size_t qe = align_up(nq * 8, 256), q4 = align_up(nq * 4, 256);
+  const size_t q4 = align_up(nq * 4, 256), qp4 = align_up((nq + 1) * 4, 256);
   const size_t rec = align_up((size_t)BFS_MAX_RECORDED_LEVELS * 4, 256);
-  g->ws_bytes = 2 * bm + 2 * (qe + 2 * q4) + 3 * rec;
+  g->ws_bytes = 2 * bm + 2 * (2 * q4 + qp4) + 3 * rec;
   CK(cudaMalloc(&g->ws, g->ws_bytes));
   char *p = (char *)g->ws;
   BfsDevState &s = g->tmpl;
@@ -116,8 +117,8 @@ static bfs_status setup_workspace(bfs_graph *g) {
   s.vis = (uint32_t *)p; p += bm;
   s.prev = (uint32_t *)p; p += bm;
   for (int b = 0; b < 2; b++) {
-    s.qe[b] = (uint2 *)p; p += qe;
-    s.qp[b] = (uint32_t *)p; p += q4;
+    s.qb[b] = (uint32_t *)p; p += q4;
+    s.qp[b] = (uint32_t *)p; p += qp4;
     s.qv[b] = (uint32_t *)p; p += q4;
   }
   s.rec_frontier = (uint32_t *)p; p += rec;
@@ -131,11 +132,13 @@ static bfs_status setup_workspace(bfs_graph *g) {
   CK(cudaMallocHost(&g->h_st, sizeof(BfsDevState)));
 
   // persistent grid sizes (occupancy x SMs)
-  for (int arm = 0; arm < kNumArms; arm++) {
-    int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, explore_kernel_fn(arm),
-                                                     arm_block(arm), 0));
-    g->occ[arm] = std::max(occ, 1);
+  for (int u = 0; u < 2; u++) {
+    for (int arm = 0; arm < kNumArms; arm++) {
+      int occ = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, explore_kernel_fn(arm, u ? 8 : 4),
+                                                       arm_block(arm), 0));
+      g->occ[u][arm] = std::max(occ, 1);
+    }
   }
   int occ_lg = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
@@ -252,23 +255,35 @@ bfs_status graph_download_impl(const bfs_graph *g, bfs_csc_host *out) {
 
 // ---- launch geometry -----------------------------------------------------------
 
-static int persistent_blocks(const bfs_graph *g, int arm, int sm_factor) {
-  int per_sm = g->occ[arm];
+static int persistent_blocks(const bfs_graph *g, int arm, int sm_factor, int ipt) {
+  int per_sm = g->occ[ipt == 8 ? 1 : 0][arm];
   if (sm_factor > 0) per_sm = sm_factor;
   return std::max(1, g->num_sms * per_sm);
 }
 
 // Grid for a host-driven launch with known frontier F (entries) and EF (edges).
-static int host_blocks(const bfs_graph *g, int arm, int sm_factor, uint32_t F, uint32_t EF) {
+static int host_blocks(const bfs_graph *g, int arm, int sm_factor, int ipt, uint32_t F,
+                       uint32_t EF) {
   const int B = arm_block(arm);
   uint64_t want;
   if (arm_lb(arm) == BFS_LB_GLB) {
-    const uint64_t chunks = ((uint64_t)EF + kGlbChunkEdges - 1) / kGlbChunkEdges;
+    const uint64_t chunks = ((uint64_t)EF + glb_chunk_edges(ipt) - 1) / glb_chunk_edges(ipt);
     want = (chunks + (B / 32) - 1) / (B / 32);
   } else {
     want = ((uint64_t)F + B - 1) / B;
   }
-  return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, persistent_blocks(g, arm, sm_factor)));
+  return (int)std::max<uint64_t>(
+      1, std::min<uint64_t>(want, persistent_blocks(g, arm, sm_factor, ipt)));
+}
+
+cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32_t F,
+                           uint32_t EF, bool persistent) {
+  BfsDevState *st = g->d_st;
+  void *args[] = {&st};
+  const int grid = persistent ? persistent_blocks(g, arm, sm_factor, ipt)
+                              : host_blocks(g, arm, sm_factor, ipt, F, EF);
+  return cudaLaunchKernel(explore_kernel_fn(arm, ipt), dim3(grid), dim3(arm_block(arm)), args, 0,
+                          g->stream);
 }
 
 static void set_window(const bfs_graph *g, cudaGraphNode_t node) {
@@ -292,10 +307,13 @@ static cudaError_t add_kernel(cudaGraph_t graph, cudaGraphNode_t *node,
   return cudaGraphAddKernelNode(node, graph, deps, ndeps, &kp);
 }
 
-// Builds the device-side level loop for a fixed explore arm:
+// Builds the device-side level loop:
 //   memset(bitmaps) -> fill(levels/parents) -> init(root) -> while(F > 0) {
 //     explore<arm> -> levelgen (last block sets the while condition) }
-static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, GraphEntry *ge) {
+// With arm < 0 (learned schedule) the body is
+//     sched (sets the switch value) -> switch(arm) { 9 explore kernels } -> levelgen
+static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt,
+                                   GraphEntry *ge) {
   cudaGraph_t graph = nullptr;
   CK(cudaGraphCreate(&graph, 0));
   ge->graph = graph;
@@ -331,9 +349,34 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, GraphEn
   cudaGraph_t body = wp.conditional.phGraph_out[0];
 
   void *ex_args[] = {&st};
-  CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm),
-                persistent_blocks(g, arm, sm_factor), arm_block(arm), ex_args));
-  set_window(g, n_explore);
+  if (arm >= 0) {
+    CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt),
+                  persistent_blocks(g, arm, sm_factor, ipt), arm_block(arm), ex_args));
+    set_window(g, n_explore);
+  } else {
+    cudaGraphConditionalHandle sw;
+    CK(cudaGraphConditionalHandleCreate(&sw, body, 0, cudaGraphCondAssignDefault));
+    unsigned long long sw_arg = (unsigned long long)sw;
+    const float *w = g->sched ? g->sched->d_w : nullptr;
+    float min_conf = g->sched ? g->sched->min_conf : 0.f;
+    SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
+    cudaGraphNode_t n_sched;
+    void *sc_args[] = {&st, &w, &min_conf, &gc, &sw_arg, &one};
+    CK(add_kernel(body, &n_sched, nullptr, 0, sched_kernel_fn(), 1, 32, sc_args));
+    alignas(cudaGraphNodeParams) unsigned char sbuf[sizeof(cudaGraphNodeParams)] = {};
+    cudaGraphNodeParams &sp = *reinterpret_cast<cudaGraphNodeParams *>(sbuf);
+    sp.type = cudaGraphNodeTypeConditional;
+    sp.conditional.handle = sw;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = kNumArms;
+    CK(cudaGraphAddNode(&n_explore, body, &n_sched, nullptr, 1, &sp));
+    for (int a = 0; a < kNumArms; a++) {
+      cudaGraphNode_t n_arm;
+      CK(add_kernel(sp.conditional.phGraph_out[a], &n_arm, nullptr, 0, explore_kernel_fn(a, ipt),
+                    persistent_blocks(g, a, sm_factor, ipt), arm_block(a), ex_args));
+      set_window(g, n_arm);
+    }
+  }
   void *lg_args[] = {&st, &cond_arg, &one};
   CK(add_kernel(body, &n_lg, &n_explore, 1, levelgen_kernel_fn(), g->lg_grid, kLevelgenBlock,
                 lg_args));
@@ -342,15 +385,16 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, GraphEn
   return BFS_OK;
 }
 
-static bfs_status get_loop_graph(bfs_graph *g, int arm, int sm_factor, GraphEntry **out) {
-  const int key = arm * 1024 + sm_factor + (g->use_l2_pin ? 512 : 0);
+static bfs_status get_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt,
+                                 GraphEntry **out) {
+  const int key = (arm + 1) * 4096 + (ipt == 8 ? 2048 : 0) + (g->use_l2_pin ? 1024 : 0) + sm_factor;
   auto it = g->graphs.find(key);
   if (it != g->graphs.end()) {
     *out = &it->second;
     return BFS_OK;
   }
   GraphEntry ge;
-  bfs_status rc = build_loop_graph(g, arm, sm_factor, &ge);
+  bfs_status rc = build_loop_graph(g, arm, sm_factor, ipt, &ge);
   if (rc != BFS_OK) {
     if (ge.exec) cudaGraphExecDestroy(ge.exec);
     if (ge.graph) cudaGraphDestroy(ge.graph);
@@ -369,11 +413,26 @@ static bfs_status read_state(bfs_graph *g) {
   return BFS_OK;
 }
 
-static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, LevelTimer *timer) {
+static bfs_status launch_sched(bfs_graph *g) {
+  BfsDevState *st = g->d_st;
+  const float *w = g->sched ? g->sched->d_w : nullptr;
+  float min_conf = g->sched ? g->sched->min_conf : 0.f;
+  SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
+  unsigned long long no_cond = 0;
+  int zero = 0;
+  void *args[] = {&st, &w, &min_conf, &gc, &no_cond, &zero};
+  CK(cudaLaunchKernel(sched_kernel_fn(), dim3(1), dim3(32), args, 0, g->stream));
+  return BFS_OK;
+}
+
+// arm_fixed < 0: the learned scheduler picks every level's arm on the device.
+static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, int ipt,
+                            LevelTimer *timer) {
   BfsDevState *st = g->d_st;
   unsigned long long no_cond = 0;
   int zero = 0;
   const bool prof = g->prof_explore != nullptr;
+  const bool learned = arm_fixed < 0;
   void *fill_args[] = {&st};
   CK(cudaMemsetAsync(g->ws, 0, g->bitmap_bytes, g->stream));
   CK(cudaLaunchKernel(fill_kernel_fn(), dim3(g->num_sms * 4), dim3(256), fill_args, 0, g->stream));
@@ -381,6 +440,11 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, LevelTim
   CK(cudaLaunchKernel(init_kernel_fn(), dim3(1), dim3(32), init_args, 0, g->stream));
   uint32_t launches = 2;
   for (uint32_t level = 0;; level++) {
+    if (learned) {
+      bfs_status rs = launch_sched(g);
+      if (rs != BFS_OK) return rs;
+      launches++;
+    }
     bfs_status rc = read_state(g);
     if (rc != BFS_OK) return rc;
     if (prof && level > 0 && level - 1 < BFS_MAX_RECORDED_LEVELS) {
@@ -389,14 +453,12 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, LevelTim
     }
     const uint32_t F = g->h_st->F, EF = g->h_st->EF;
     if (F == 0) break;
-    int arm = arm_fixed;
+    int arm = learned ? g->h_st->arm : arm_fixed;
     if (timer && timer->choose) arm = timer->choose(timer->ctx, g, level, F, EF);
     if (arm < 0 || arm >= kNumArms) return fail(BFS_ERR_INVALID_ARG, "scheduler chose a bad arm");
-    void *ex_args[] = {&st};
     if (timer && timer->before) timer->before(timer->ctx, g, level, arm);
     if (prof) CK(cudaEventRecord(g->lvl_ev[0], g->stream));
-    CK(cudaLaunchKernel(explore_kernel_fn(arm), dim3(host_blocks(g, arm, sm_factor, F, EF)),
-                        dim3(arm_block(arm)), ex_args, 0, g->stream));
+    CK(launch_explore(g, arm, ipt, sm_factor, F, EF, false));
     if (prof) CK(cudaEventRecord(g->lvl_ev[1], g->stream));
     if (timer && timer->after) timer->after(timer->ctx, g, level, arm);
     void *lg_args[] = {&st, &no_cond, &zero};
@@ -426,8 +488,8 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
   if (o.loop != BFS_LOOP_GRAPH && o.loop != BFS_LOOP_HOST)
     return fail(BFS_ERR_INVALID_ARG, "unknown loop mode");
   if (o.sm_factor < 0 || o.sm_factor > 64) return fail(BFS_ERR_INVALID_ARG, "sm_factor out of range");
-  if (o.lb == BFS_LB_LEARNED && !(timer && timer->choose) && !g->sched)
-    return fail(BFS_ERR_UNSUPPORTED, "learned scheduler selected but no model is attached");
+  if (o.ipt == 0) o.ipt = 4;
+  if (o.ipt != 4 && o.ipt != 8) return fail(BFS_ERR_INVALID_ARG, "ipt must be 4 or 8");
   CK(cudaSetDevice(g->device));
   g->use_l2_pin = o.l2_pin != 0;
   if (o.loop == BFS_LOOP_HOST) {
@@ -457,17 +519,14 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
   bfs_status rc;
   uint32_t launches = 0;
   bool host_driven = false;
-  if (o.lb == BFS_LB_LEARNED) {
-    rc = run_learned(g, o, timer, &launches);
-    if (rc != BFS_OK) return rc;
-  } else if (o.loop == BFS_LOOP_GRAPH && !timer && o.record < 2) {
+  if (o.loop == BFS_LOOP_GRAPH && !timer && o.record < 2) {
     GraphEntry *ge = nullptr;
-    rc = get_loop_graph(g, arm, o.sm_factor, &ge);
+    rc = get_loop_graph(g, arm, o.sm_factor, o.ipt, &ge);
     if (rc != BFS_OK) return rc;
     CK(cudaGraphLaunch(ge->exec, g->stream));
   } else {
     host_driven = true;
-    rc = host_loop(g, arm, o.sm_factor, timer);
+    rc = host_loop(g, arm, o.sm_factor, o.ipt, timer);
     if (rc != BFS_OK) return rc;
     launches = g->host_launches;
   }
@@ -544,6 +603,7 @@ void bfs_options_default(bfs_options *o) {
   o->loop = BFS_LOOP_GRAPH;
   o->l2_pin = 1;
   o->record = 0;
+  o->ipt = 4;
 }
 
 static bfs_status require_device() {

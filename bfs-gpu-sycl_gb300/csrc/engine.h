@@ -29,10 +29,12 @@ struct LevelTimer {
 bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts,
                            int32_t *levels_dev, int32_t *parents_dev, bfs_stats *stats,
                            LevelTimer *timer);
-// learned-scheduler level loop (sched.cu)
-bfs_status run_learned(bfs_graph *g, const bfs_options &o, LevelTimer *timer,
-                       uint32_t *launches);
-void free_sched(bfs_graph *g);
+// Launches one explore kernel on the handle's stream for a frontier of F
+// entries and EF edges; persistent = full persistent grid (as in the graph
+// loop) instead of a grid sized to the frontier.
+cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32_t F,
+                           uint32_t EF, bool persistent);
+void free_sched(bfs_graph *g);  // bfs_sched.cu
 
 }  // namespace bfsgb
 
@@ -58,7 +60,7 @@ struct bfs_graph {
   cudaEvent_t lvl_ev[3] = {nullptr, nullptr, nullptr};  // per-level kernel timing
   float *prof_explore = nullptr;  // host arrays filled by the host loop (record == 2)
   float *prof_gen = nullptr;
-  int occ[bfsgb::kNumArms] = {};
+  int occ[2][bfsgb::kNumArms] = {};  // blocks per SM, [ipt == 8][arm]
   int lg_grid = 0;
   bool l2_pinned = false;
   bool use_l2_pin = true;

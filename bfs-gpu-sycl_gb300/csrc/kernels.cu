@@ -62,8 +62,12 @@ __device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent
                                       uint32_t from) {
   const uint32_t w = n >> 5, bit = 1u << (n & 31u);
   if (vis[w] & bit) return;
-  const uint32_t old = atomicOr(vis + w, bit);
-  if (parent && !(old & bit)) parent[n] = (int32_t)from;
+  if (parent) {
+    const uint32_t old = atomicOr(vis + w, bit);
+    if (!(old & bit)) parent[n] = (int32_t)from;
+  } else {
+    atomicOr(vis + w, bit);  // result unused: a reduction, no round trip
+  }
 }
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, uint32_t lane) {
@@ -131,12 +135,14 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
     e = st->indptr[r + 1];
   }
   if (expanded && e > b) {
-    st->qe[0][0] = make_uint2(b, e);
+    st->qb[0][0] = b;
     st->qp[0][0] = 0;
+    st->qp[0][1] = e - b;
     st->qv[0][0] = r;
     st->F = 1;
     st->EF = e - b;
   } else {
+    st->qp[0][0] = 0;
     st->F = 0;
     st->EF = 0;
   }
@@ -165,7 +171,8 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
 // number of tiles, the strided mapping of run_bfs_gpu.hpp:416-420.  A block
 // exclusive scan of the tile's degrees (shared memory) splits the tile's
 // edges evenly over the block's warps (block-local balancing, :437-445).
-template <int B, bool STRIDED>
+// U warp rounds (U edges per lane) are resolved before their loads issue.
+template <int B, bool STRIDED, int U>
 __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
   __shared__ uint32_t s_off[B + 1];
@@ -176,7 +183,8 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t cur_q = st->cur;
-  const uint2 *__restrict__ qe = st->qe[cur_q];
+  const uint32_t *__restrict__ qb = st->qb[cur_q];
+  const uint32_t *__restrict__ qp = st->qp[cur_q];
   const uint32_t *__restrict__ qv = st->qv[cur_q];
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
@@ -189,9 +197,8 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
     const uint32_t slot = STRIDED ? tile + threadIdx.x * num_tiles : tile * B + threadIdx.x;
     uint32_t beg = 0, deg = 0, vid = 0;
     if (slot < F) {
-      const uint2 e = qe[slot];
-      beg = e.x;
-      deg = e.y - e.x;
+      beg = qb[slot];
+      deg = qp[slot + 1] - qp[slot];
       if (parent) vid = qv[slot];
     }
     const uint32_t incl = warp_incl_scan(deg, lane);
@@ -223,32 +230,30 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
         if (s_off[mid] <= w0) lo = mid; else hi = mid;
       }
       uint32_t cur = lo;
-      for (uint32_t base = w0; base < w1; base += 32u * kUnroll) {
-        uint32_t addr[kUnroll], from[kUnroll];
-        bool act[kUnroll];
+      for (uint32_t base = w0; base < w1; base += 32u * U) {
+        uint32_t addr[U], from[U];
 #pragma unroll
-        for (int u = 0; u < kUnroll; u++) {
+        for (int u = 0; u < U; u++) {
           const uint32_t rb = base + 32u * u;
           const uint32_t e = rb + lane;
           const uint32_t j = cur + 1u + lane;
           const uint32_t bnd = (j <= (uint32_t)B) ? s_off[j] : kFull;
           const uint32_t o = round_owner(cur, bnd, rb, lane);
-          act[u] = (rb < w1) && (e < w1);
-          addr[u] = 0;
+          addr[u] = kFull;
           from[u] = 0;
-          if (act[u]) {
+          if (e < w1) {
             addr[u] = s_beg[o] + (e - s_off[o]);
             from[u] = s_vid[o];
           }
           cur = __shfl_sync(kFull, o, 31);
           if (cur >= (uint32_t)B) cur = B - 1;  // only reached past w1
         }
-        uint32_t nb[kUnroll];
+        uint32_t nb[U];
 #pragma unroll
-        for (int u = 0; u < kUnroll; u++) nb[u] = act[u] ? ld_stream(inds + addr[u], pol) : 0u;
+        for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
 #pragma unroll
-        for (int u = 0; u < kUnroll; u++)
-          if (act[u]) visit(vis, nb[u], parent, from[u]);
+        for (int u = 0; u < U; u++)
+          if (addr[u] != kFull) visit(vis, nb[u], parent, from[u]);
       }
     }
     __syncthreads();
@@ -261,13 +266,13 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
 // SMs*SM_FACTOR work-groups).  The grid-wide exclusive scan of degrees is the
 // queue's prefix array written by level generation (EN1-EN3, :203-307).
 // A warp finds the owner of its chunk start with a 32-ary search of the scan
-// (one probe per lane and round), then resolves owners per round like LLB.
-constexpr uint32_t kGlbChunk = kGlbChunkEdges;
-
+// (one probe per lane and round), then walks forward: each round loads the
+// next 32 entry starts and first-edge offsets coalesced, and every lane takes
+// its owner's offsets from those registers with shuffles.
 __device__ __forceinline__ uint32_t warp_owner_search(const uint32_t *__restrict__ qp,
                                                       uint32_t F, uint32_t x,
                                                       uint32_t lane) {
-  uint32_t lo = 0, hi = F;  // qp[lo] <= x < qp[hi] (qp[F] = +inf)
+  uint32_t lo = 0, hi = F;  // qp[lo] <= x < qp[hi] (qp[F] = edge total)
   while (hi - lo > 32u) {
     const uint32_t step = (hi - lo + 31u) >> 5;
     const uint32_t j = lo + lane * step;
@@ -283,14 +288,15 @@ __device__ __forceinline__ uint32_t warp_owner_search(const uint32_t *__restrict
   return lo + 31u - __clz(m);
 }
 
-template <int B>
+template <int B, int U>
 __global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
+  constexpr uint32_t CHUNK = 32u * U * kGlbGroups;  // edges per warp chunk
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t EF = st->EF;
   const uint32_t cur_q = st->cur;
-  const uint2 *__restrict__ qe = st->qe[cur_q];
+  const uint32_t *__restrict__ qb = st->qb[cur_q];
   const uint32_t *__restrict__ qp = st->qp[cur_q];
   const uint32_t *__restrict__ qv = st->qv[cur_q];
   const uint32_t *__restrict__ inds = st->inds;
@@ -298,39 +304,53 @@ __global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restri
   int32_t *parent = st->parent;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
-  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + kGlbChunk - 1) / kGlbChunk);
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
   const uint32_t total_warps = gridDim.x * NW;
 
   for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
-    const uint32_t w0 = c * kGlbChunk;
-    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + kGlbChunk);
+    const uint32_t w0 = c * CHUNK;
+    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
-    for (uint32_t base = w0; base < w1; base += 32u * kUnroll) {
-      uint32_t addr[kUnroll], from[kUnroll];
-      bool act[kUnroll];
+    uint32_t cur_start = qp[cur], cur_beg = qb[cur];
+    uint32_t cur_vid = parent ? qv[cur] : 0u;
+    for (uint32_t base = w0; base < w1; base += 32u * U) {
+      uint32_t addr[U], from[U];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) {
+      for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
         const uint32_t e = rb + lane;
         const uint32_t j = cur + 1u + lane;
-        const uint32_t bnd = (j < F) ? qp[j] : (j == F ? EF : kFull);
-        const uint32_t o = round_owner(cur, bnd, rb, lane);
-        act[u] = (rb < w1) && (e < w1);
-        addr[u] = 0;
+        const uint32_t bnd = (j <= F) ? qp[j] : kFull;  // qp[F] = EF
+        const uint32_t bg = (j < F) ? qb[j] : 0u;
+        const uint32_t vd = (parent && j < F) ? qv[j] : 0u;
+        const uint32_t p = bnd - rb;
+        const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
+        const uint32_t k = __popc(starts & ((2u << lane) - 1u));
+        const uint32_t srcl = k ? k - 1u : 0u;
+        const uint32_t s_start = __shfl_sync(kFull, bnd, srcl);
+        const uint32_t s_beg = __shfl_sync(kFull, bg, srcl);
+        const uint32_t s_vid = __shfl_sync(kFull, vd, srcl);
+        addr[u] = kFull;
         from[u] = 0;
-        if (act[u]) {
-          addr[u] = qe[o].x + (e - qp[o]);
-          if (parent) from[u] = qv[o];
+        if (e < w1) {
+          addr[u] = (k ? s_beg : cur_beg) + (e - (k ? s_start : cur_start));
+          from[u] = k ? s_vid : cur_vid;
         }
-        cur = __shfl_sync(kFull, o, 31);
-        if (cur >= F) cur = F - 1;  // only reached past w1
+        // carry the owner of lane 31 into the next round
+        const uint32_t k31 = __shfl_sync(kFull, k, 31);
+        if (k31) {
+          cur += k31;
+          cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
+          cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
+          cur_vid = __shfl_sync(kFull, vd, k31 - 1u);
+        }
       }
-      uint32_t nb[kUnroll];
+      uint32_t nb[U];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) nb[u] = act[u] ? ld_stream(inds + addr[u], pol) : 0u;
+      for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++)
-        if (act[u]) visit(vis, nb[u], parent, from[u]);
+      for (int u = 0; u < U; u++)
+        if (addr[u] != kFull) visit(vis, nb[u], parent, from[u]);
     }
   }
 }
@@ -345,7 +365,9 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
   if (reached > st->reached_prev) st->max_level = lvl;
   st->reached_prev = reached;
   st->edges_count += ef_new;
-  st->cur ^= 1u;
+  const uint32_t nq = st->cur ^ 1u;
+  st->qp[nq][f_new] = ef_new;  // trailing total of the new queue's scan
+  st->cur = nq;
   st->F = f_new;
   st->EF = ef_new;
   st->lvl = lvl;
@@ -382,7 +404,7 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
   const int32_t lvl_next = (int32_t)st->lvl + 1;
   int32_t *__restrict__ level = st->level;
   const uint32_t nq = st->cur ^ 1u;
-  uint2 *__restrict__ qe = st->qe[nq];
+  uint32_t *__restrict__ qb = st->qb[nq];
   uint32_t *__restrict__ qp = st->qp[nq];
   uint32_t *__restrict__ qv = st->qv[nq];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -447,7 +469,7 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
         const uint32_t dx = warp_incl_scan(deg, lane) - deg;
         if (deg) {
           const uint32_t slot = (uint32_t)(wbase >> 32) + __popc(km & lt_mask);
-          qe[slot] = make_uint2(b, e);
+          qb[slot] = b;
           qp[slot] = (uint32_t)wbase + dx;
           qv[slot] = v;
         }
@@ -476,25 +498,36 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
 }
 
 // ---- validation (Graph500-style checks of a level array) --------------------
-// Edge pass: for every expanded reached u and edge u->v: level[v] must be
-// reached and <= level[u] + 1; v gets a witness if level[v] == level[u] + 1,
-// and its parent is confirmed if parent[v] == u.
+// Edge pass, edge-balanced: each thread takes kValEdges consecutive edges,
+// finds the first one's source by binary search over indptr and walks on.
+// For every expanded reached u and edge u->v: level[v] must be reached and
+// <= level[u] + 1; v gets a witness if level[v] == level[u] + 1, and its
+// parent is confirmed if parent[v] == u.
+constexpr uint32_t kValEdges = 16;
+
 __global__ void validate_edges_kernel(const uint32_t *__restrict__ indptr,
                                       const uint32_t *__restrict__ inds, uint32_t n_rows,
                                       const int32_t *__restrict__ level,
                                       const int32_t *__restrict__ parent,
                                       uint8_t *witness, uint8_t *parent_ok,
                                       unsigned long long *bad) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  unsigned long long nbad = 0;
-  for (uint32_t u = gwarp; u < n_rows; u += nwarps) {
-    const int32_t lu = level[u];
-    if (lu < 0) continue;
-    const uint32_t b = indptr[u], e = indptr[u + 1];
-    for (uint32_t k = b + lane; k < e; k += 32u) {
-      const uint32_t v = inds[k];
+  const uint32_t total = indptr[n_rows];  // edges of expandable vertices
+  uint32_t nbad = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kValEdges;
+  for (uint64_t e0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kValEdges;
+       e0 < total; e0 += stride) {
+    uint32_t lo = 0, hi = n_rows;  // last u with indptr[u] <= e0
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (indptr[mid] <= e0) lo = mid; else hi = mid;
+    }
+    uint32_t u = lo;
+    const uint32_t e1 = (uint32_t)min((uint64_t)total, e0 + kValEdges);
+    for (uint32_t e = (uint32_t)e0; e < e1; e++) {
+      while (indptr[u + 1] <= e) u++;
+      const int32_t lu = level[u];
+      if (lu < 0) continue;
+      const uint32_t v = inds[e];
       const int32_t lv = level[v];
       if (lv < 0 || lv > lu + 1) nbad++;
       if (lv == lu + 1) {
@@ -503,8 +536,8 @@ __global__ void validate_edges_kernel(const uint32_t *__restrict__ indptr,
       }
     }
   }
-  nbad = __reduce_add_sync(kFull, (uint32_t)nbad);
-  if (lane == 0 && nbad) atomicAdd(bad, nbad);
+  nbad = __reduce_add_sync(kFull, nbad);
+  if ((threadIdx.x & 31u) == 0 && nbad) atomicAdd(bad, (unsigned long long)nbad);
 }
 
 // Vertex pass: root at level 0 (and its own parent); any other reached vertex
@@ -552,19 +585,23 @@ __global__ void check_csc_kernel(const uint32_t *__restrict__ indptr,
 }
 
 // ---- kernel table ---------------------------------------------------------
-const void *explore_kernel_fn(int arm) {
+template <int U>
+static const void *explore_fn_u(int arm) {
   switch (arm) {
-    case 0: return (const void *)explore_local_kernel<128, false>;
-    case 1: return (const void *)explore_local_kernel<256, false>;
-    case 2: return (const void *)explore_local_kernel<512, false>;
-    case 3: return (const void *)explore_global_kernel<128>;
-    case 4: return (const void *)explore_global_kernel<256>;
-    case 5: return (const void *)explore_global_kernel<512>;
-    case 6: return (const void *)explore_local_kernel<128, true>;
-    case 7: return (const void *)explore_local_kernel<256, true>;
-    case 8: return (const void *)explore_local_kernel<512, true>;
+    case 0: return (const void *)explore_local_kernel<128, false, U>;
+    case 1: return (const void *)explore_local_kernel<256, false, U>;
+    case 2: return (const void *)explore_local_kernel<512, false, U>;
+    case 3: return (const void *)explore_global_kernel<128, U>;
+    case 4: return (const void *)explore_global_kernel<256, U>;
+    case 5: return (const void *)explore_global_kernel<512, U>;
+    case 6: return (const void *)explore_local_kernel<128, true, U>;
+    case 7: return (const void *)explore_local_kernel<256, true, U>;
+    case 8: return (const void *)explore_local_kernel<512, true, U>;
     default: return nullptr;
   }
+}
+const void *explore_kernel_fn(int arm, int ipt) {
+  return ipt == 8 ? explore_fn_u<8>(arm) : explore_fn_u<4>(arm);
 }
 const void *levelgen_kernel_fn() { return (const void *)levelgen_kernel<kLevelgenBlock>; }
 const void *init_kernel_fn() { return (const void *)init_kernel; }

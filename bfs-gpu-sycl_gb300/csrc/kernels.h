@@ -8,13 +8,16 @@
 namespace bfsgb {
 
 constexpr int kLevelgenBlock = 256;
-constexpr int kUnroll = 4;                          // warp rounds in flight per warp
-constexpr uint32_t kGlbChunkEdges = 32u * kUnroll * 2u;  // GLB edges per warp chunk
+// Explore kernels keep U warp rounds (U edges per lane) in flight; U is the
+// "items per thread" tunable (4 or 8).  A GLB warp chunk is kGlbGroups groups
+// of U rounds.
+constexpr int kGlbGroups = 4;
+inline uint32_t glb_chunk_edges(int ipt) { return 32u * (uint32_t)ipt * kGlbGroups; }
 
 // Kernel function pointers (for CUDA-graph kernel nodes and direct launches).
 // Every kernel takes (BfsDevState*) first; levelgen and init also take
 // (unsigned long long conditional_handle, int use_conditional).
-const void *explore_kernel_fn(int arm);
+const void *explore_kernel_fn(int arm, int ipt);
 const void *levelgen_kernel_fn();
 const void *init_kernel_fn();
 const void *fill_kernel_fn();

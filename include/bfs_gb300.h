@@ -76,6 +76,8 @@ typedef struct bfs_options {
   int32_t l2_pin;      /* 1 = pin the visited bitmaps in L2 (default on) */
   int32_t record;      /* 1 = fill bfs_stats per-level arrays; 2 = also time
                           every kernel with CUDA events (forces the host loop) */
+  int32_t ipt;         /* edges per lane in flight in the explore kernels:
+                          4 or 8 (0 = 4) */
 } bfs_options;
 
 #define BFS_MAX_RECORDED_LEVELS 4096
@@ -144,6 +146,59 @@ bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,
  * number of violations (0 = valid). */
 bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,
                                const int32_t *parents_dev, uint64_t *bad);
+
+/* ---- learned per-level scheduler -------------------------------------- */
+/* The reference fixes the load-balancing form and work-group size at compile
+ * time (src/CMakeLists.txt:10-11; run_bfs_gpu.hpp:195, 403, 493).  Here a
+ * small FP32 MLP picks the explore arm (lb * 3 + block index, 9 arms) for
+ * every level from 5 features of the level:
+ *   x0 = log2(1 + frontier vertices) / 32
+ *   x1 = log2(1 + frontier edges) / 32
+ *   x2 = unvisited fraction (1 - reached / n_cols)
+ *   x3 = min(level / diameter estimate, 8) / 8, with the estimate
+ *        max(2, ln(n_cols) / ln(max(average degree, 2)))
+ *   x4 = log2(1 + average degree nnz / n_cols) / 8
+ * Layers 5 -> 32 (ReLU) -> 32 (ReLU) -> 9, softmax; weights are 1545 floats
+ * laid out W1[32][5], b1[32], W2[32][32], b2[32], W3[9][32], b3[9].
+ * Inference runs on the device inside the level loop; the choice never
+ * changes the levels, only the time. */
+#define BFS_SCHED_INPUTS 5
+#define BFS_SCHED_ARMS 9
+#define BFS_SCHED_PARAMS 1545
+
+typedef struct bfs_level_sample {
+  float features[BFS_SCHED_INPUTS];
+  float arm_ms[BFS_SCHED_ARMS];   /* explore time of every arm on this level */
+  uint32_t level, frontier, edges;
+} bfs_level_sample;
+
+typedef struct bfs_sched_train_opts {
+  uint32_t epochs;      /* full-batch Adam steps (0 = 1500) */
+  float lr;             /* Adam step size (0 = 3e-3) */
+  uint64_t seed;        /* weight initialisation seed */
+} bfs_sched_train_opts;
+
+/* Runs one BFS from root in the host loop and, on every level, times the
+ * explore step of all 9 arms (state restored between arms, best of `reps`
+ * repetitions) before advancing.  Fills out[0 .. *n_out). */
+bfs_status bfs_sched_record(bfs_graph *g, uint32_t root, int32_t ipt, int32_t reps,
+                            bfs_level_sample *out, uint32_t max_levels, uint32_t *n_out);
+/* Trains the MLP on the current CUDA device (hand-written forward/backward
+ * and Adam kernels).  The loss is the expected excess explore time
+ * sum_a softmax(z)_a * (t_a - t_best), in units of the mean best time, so
+ * the fit minimises per-level regret.  weights_out receives 1545 floats. */
+bfs_status bfs_sched_train(const bfs_level_sample *samples, uint32_t n,
+                           const bfs_sched_train_opts *opts, float *weights_out,
+                           float *final_loss);
+/* Device inference on n feature vectors (n x 5): arms_out[i] = argmax arm,
+ * conf_out[i] = its softmax probability (either output may be NULL). */
+bfs_status bfs_sched_predict(const float *weights, const float *features, uint32_t n,
+                             int32_t *arms_out, float *conf_out);
+/* Attaches a model to a graph handle for bfs_options.lb = BFS_LB_LEARNED.
+ * Levels whose top probability is below min_confidence fall back to the
+ * fixed LLB/256 arm; with no model attached every level uses LLB/256.
+ * weights == NULL detaches. */
+bfs_status bfs_sched_attach(bfs_graph *g, const float *weights, float min_confidence);
 
 /* ---- synthetic graphs and roots --------------------------------------- */
 /* Seeded generators.  Every edge is a pure function of (seed, index) through

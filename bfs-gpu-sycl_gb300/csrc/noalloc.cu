@@ -1,0 +1,195 @@
+// noalloc.cu -- single-root BFS that allocates no memory.
+//
+// Some callers cannot call cudaMalloc: code running inside an allocator or a
+// memory-pool callback (a cudaMalloc there could re-enter it), processes that
+// run under a hard device-memory budget fixed at start-up, and plugins whose
+// host forbids device allocation after initialisation.  bfs_run_device_noalloc
+// serves them: the caller passes the graph and the output level array (device
+// memory it already owns), and the BFS workspace -- visited bitmaps, the two
+// frontier queues and the level-loop state -- lives in the file-scope device
+// array below.  It is sized for graphs of at most BFS_NOALLOC_MAX_VERTICES
+// vertices (about 24 MiB), and every GPU that loads this library keeps it
+// until the process exits.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address with cudaGetSymbolAddress (the name of the array in
+// host code is a host-side stand-in, not a device address, so it is never
+// passed to a kernel).  Make that first call before any stream capture.
+//
+// Sharing: every call on a device uses the same array, and the array keeps the
+// previous call's contents; each call clears the parts that must start at zero
+// (both bitmaps and the loop counters).  Two calls that overlap on the GPU --
+// from two host threads, or on two streams -- race on the array; serialise
+// them.
+//
+// No cudaMalloc, cudaFree or other allocating routine is called: the launch
+// geometry comes from an occupancy query, the state is written by a kernel
+// from its by-value argument, and the per-level frontier size is read back
+// with a small device-to-host copy.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "bfs_internal.h"
+#include "kernels.h"
+
+namespace bfsgb {
+namespace {
+
+constexpr uint32_t kMaxV = BFS_NOALLOC_MAX_VERTICES;
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+// layout of the scratch array
+constexpr size_t kStateOff = 0;
+constexpr size_t kBadOff = align256(sizeof(BfsDevState));
+constexpr size_t kWordsMax = (((size_t)kMaxV + 31) / 32 + 31) / 32 * 32;
+constexpr size_t kVisOff = kBadOff + 256;
+constexpr size_t kPrevOff = kVisOff + align256(kWordsMax * 4);
+constexpr size_t kQ4 = align256((size_t)kMaxV * 4);
+constexpr size_t kQp4 = align256(((size_t)kMaxV + 1) * 4);
+constexpr size_t kQOff = kPrevOff + align256(kWordsMax * 4);
+constexpr size_t kScratchBytes = kQOff + 2 * (2 * kQ4 + kQp4);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char *g_scratch_dev[kMaxDevices] = {};
+int g_grid[kMaxDevices][2] = {};  // explore, levelgen grid per device
+
+constexpr int kArm = 4;  // GLB, 256 threads
+constexpr int kIpt = 4;
+
+// Writes the loop state from its by-value argument and clears the error
+// counter (no host-to-device copy of a host buffer is needed).
+__global__ void noalloc_state_kernel(BfsDevState s, BfsDevState *dst,
+                                     unsigned long long *bad) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *dst = s;
+    *bad = 0ull;
+  }
+}
+
+bfs_status setup_device(int dev) {
+  std::lock_guard<std::mutex> lk(g_setup_mutex);
+  if (g_scratch_dev[dev]) return BFS_OK;
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(BFS_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
+                                  cudaGetErrorString(e));
+  int sms = 0, occ_ex = 0, occ_lg = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, explore_kernel_fn(kArm, kIpt),
+                                                      arm_block(kArm), 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
+                                                      kLevelgenBlock, 0);
+  if (e != cudaSuccess)
+    return fail(BFS_ERR_CUDA, std::string("launch geometry: ") + cudaGetErrorString(e));
+  g_grid[dev][0] = sms * (occ_ex > 0 ? occ_ex : 1);
+  g_grid[dev][1] = sms * (occ_lg > 0 ? occ_lg : 1);
+  g_scratch_dev[dev] = (unsigned char *)p;
+  return BFS_OK;
+}
+
+}  // namespace
+}  // namespace bfsgb
+
+using namespace bfsgb;
+
+#define NK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(BFS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uint32_t *d_inds,
+                                             uint32_t n_rows, uint32_t n_cols, uint64_t nnz,
+                                             uint32_t root, int32_t *levels_dev,
+                                             uint64_t *edges_count_out, void *stream) {
+  if (!d_indptr || (!d_inds && nnz) || !levels_dev)
+    return fail(BFS_ERR_INVALID_ARG, "null graph or level buffer");
+  if (n_cols == 0 || n_rows > n_cols)
+    return fail(BFS_ERR_INVALID_ARG, "need 0 < n_cols and n_rows <= n_cols");
+  if (n_cols > kMaxV)
+    return fail(BFS_ERR_INVALID_ARG,
+                "bfs_run_device_noalloc supports at most " + std::to_string(kMaxV) +
+                    " vertices (its fixed scratch size); use bfs_run_device for larger graphs");
+  if (nnz > 0xFFFFFFFFull) return fail(BFS_ERR_INVALID_ARG, "nnz must fit uint32 offsets");
+  if (root >= n_cols) return fail(BFS_ERR_ROOT, "root out of range");
+  int dev = 0;
+  NK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(BFS_ERR_UNSUPPORTED, "device index too large");
+  bfs_status rc = setup_device(dev);
+  if (rc != BFS_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char *base = g_scratch_dev[dev];
+
+  BfsDevState h;
+  std::memset(&h, 0, sizeof(h));
+  h.indptr = d_indptr;
+  h.inds = d_inds;
+  h.n_rows = n_rows;
+  h.n_cols = n_cols;
+  h.words = (uint32_t)((((size_t)n_cols + 31) / 32 + 31) / 32 * 32);
+  h.root = root;
+  h.vis = (uint32_t *)(base + kVisOff);
+  h.prev = (uint32_t *)(base + kPrevOff);
+  for (int b = 0; b < 2; b++) {
+    unsigned char *q = base + kQOff + (size_t)b * (2 * kQ4 + kQp4);
+    h.qb[b] = (uint32_t *)q;
+    h.qp[b] = (uint32_t *)(q + kQ4);
+    h.qv[b] = (uint32_t *)(q + kQ4 + kQp4);
+  }
+  h.level = levels_dev;
+  h.parent = nullptr;
+  h.fixed_arm = kArm;
+  h.level_cap = n_cols + 1u;
+  h.rec_cap = 0;  // no per-level record in this entry point
+  BfsDevState *st = (BfsDevState *)(base + kStateOff);
+  unsigned long long *bad = (unsigned long long *)(base + kBadOff);
+
+  // state + cleared counters, cleared bitmaps, CSC check
+  noalloc_state_kernel<<<1, 32, 0, s>>>(h, st, bad);
+  NK(cudaGetLastError());
+  NK(cudaMemsetAsync(h.vis, 0, (size_t)h.words * 4, s));
+  NK(cudaMemsetAsync(h.prev, 0, (size_t)h.words * 4, s));
+  NK(launch_check_csc(d_indptr, d_inds, n_cols, nnz, bad, s));
+  unsigned long long h_bad = 0;
+  NK(cudaMemcpyAsync(&h_bad, bad, sizeof(h_bad), cudaMemcpyDeviceToHost, s));
+  NK(cudaStreamSynchronize(s));
+  if (h_bad) return fail(BFS_ERR_GRAPH, "malformed CSC: " + std::to_string(h_bad) + " errors");
+
+  unsigned long long no_cond = 0;
+  int zero = 0;
+  void *fill_args[] = {&st};
+  NK(cudaLaunchKernel(fill_kernel_fn(), dim3(g_grid[dev][1]), dim3(256), fill_args, 0, s));
+  void *init_args[] = {&st, &no_cond, &zero};
+  NK(cudaLaunchKernel(init_kernel_fn(), dim3(1), dim3(32), init_args, 0, s));
+  for (;;) {
+    uint32_t F = 0;
+    NK(cudaMemcpyAsync(&F, &st->F, sizeof(F), cudaMemcpyDeviceToHost, s));
+    NK(cudaStreamSynchronize(s));
+    if (F == 0) break;
+    void *ex_args[] = {&st};
+    NK(cudaLaunchKernel(explore_kernel_fn(kArm, kIpt), dim3(g_grid[dev][0]), dim3(arm_block(kArm)),
+                        ex_args, 0, s));
+    void *lg_args[] = {&st, &no_cond, &zero};
+    NK(cudaLaunchKernel(levelgen_kernel_fn(), dim3(g_grid[dev][1]), dim3(kLevelgenBlock), lg_args,
+                        0, s));
+  }
+  uint32_t err = 0;
+  unsigned long long edges = 0;
+  NK(cudaMemcpyAsync(&err, &st->error, sizeof(err), cudaMemcpyDeviceToHost, s));
+  NK(cudaMemcpyAsync(&edges, &st->edges_count, sizeof(edges), cudaMemcpyDeviceToHost, s));
+  NK(cudaStreamSynchronize(s));
+  if (err & BFS_DEVERR_LEVEL_LIMIT)
+    return fail(BFS_ERR_LEVEL_LIMIT, "level loop exceeded n_cols + 1 levels");
+  if (err) return fail(BFS_ERR_DEVICE, "device error flag " + std::to_string(err));
+  if (edges_count_out) *edges_count_out = edges;
+  return BFS_OK;
+}

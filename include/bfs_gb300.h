@@ -147,6 +147,27 @@ bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,
 bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,
                                const int32_t *parents_dev, uint64_t *bad);
 
+/* ---- BFS without device allocation ------------------------------------ */
+/* No counterpart in the reference (its GPURun allocates per run).  For
+ * callers that cannot allocate device memory -- code inside an allocator or
+ * memory-pool callback, processes under a device-memory budget fixed at
+ * start-up, plugins whose host forbids allocation after initialisation.
+ * One BFS from root over a CSC graph already on the current device, into
+ * levels_dev (n_cols int32, caller-owned); *edges_count_out (optional, host)
+ * receives the reference's edgesCount.  The workspace is a fixed device array
+ * inside the library (about 24 MiB per GPU that loads it, held until exit),
+ * so graphs are limited to BFS_NOALLOC_MAX_VERTICES vertices and larger ones
+ * are rejected with BFS_ERR_INVALID_ARG.  The first call on a device looks
+ * up that array's address (make it before any stream capture).  All calls on
+ * a device share the array: calls that overlap on the GPU race, so serialise
+ * them.  stream may be NULL (default stream); the call returns when the BFS
+ * has finished. */
+#define BFS_NOALLOC_MAX_VERTICES (1u << 20)
+bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uint32_t *d_inds,
+                                  uint32_t n_rows, uint32_t n_cols, uint64_t nnz,
+                                  uint32_t root, int32_t *levels_dev,
+                                  uint64_t *edges_count_out, void *stream);
+
 /* ---- learned per-level scheduler -------------------------------------- */
 /* The reference fixes the load-balancing form and work-group size at compile
  * time (src/CMakeLists.txt:10-11; run_bfs_gpu.hpp:195, 403, 493).  Here a

@@ -69,6 +69,11 @@ class TrainOpts(C.Structure):
     _fields_ = [("epochs", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("batches", C.c_uint32),
+                ("max_levels", C.c_uint32), ("launches", C.c_uint32)]
+
+
 class CscHost(C.Structure):
     _fields_ = [("n_rows", C.c_uint32), ("n_cols", C.c_uint32), ("nnz", C.c_uint64),
                 ("indptr", C.POINTER(C.c_uint32)), ("inds", C.POINTER(C.c_uint32))]
@@ -130,6 +135,8 @@ def lib():
     _sig(L, "bfs_sched_predict", [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32, I32P,
                                   C.POINTER(C.c_float)])
     _sig(L, "bfs_sched_attach", [VP, C.POINTER(C.c_float), C.c_float])
+    _sig(L, "bfs_run_batch", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
+                              C.POINTER(BatchStats)])
     _lib = L
     return L
 
@@ -359,6 +366,17 @@ class Graph:
                                    VP(levels_ptr), VP(parents_ptr) if parents_ptr else None,
                                    C.byref(st) if st is not None else None))
         return st
+
+    def run_batch(self, roots, levels_ptr, want_edges=True):
+        """Multi-source BFS of len(roots) roots into a device int32 buffer of
+        len(roots) x n_cols; returns (edges uint64[len(roots)] or None, BatchStats)."""
+        rt = np.ascontiguousarray(roots, np.uint32)
+        ec = np.zeros(len(rt), np.uint64) if want_edges else None
+        st = BatchStats()
+        check(lib().bfs_run_batch(self.h, rt.ctypes.data_as(U32P), len(rt), VP(levels_ptr),
+                                  ec.ctypes.data_as(C.POINTER(C.c_uint64)) if want_edges
+                                  else None, C.byref(st)))
+        return ec, st
 
     def sched_record(self, root, ipt=4, reps=3, max_levels=1 << 16):
         """Per-level features and explore times of all 9 arms for one BFS."""

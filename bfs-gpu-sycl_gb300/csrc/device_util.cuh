@@ -1,0 +1,66 @@
+// device_util.cuh -- warp-level helpers shared by the BFS kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace bfsgb {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+// ---- device helpers ---------------------------------------------------------
+
+// Edge-array load: read once per BFS, so bypass L1 and mark evict-first in L2
+// to keep the L2 for the visited bitmaps and queues.
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p, uint64_t pol) {
+  uint32_t r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+               : "=r"(r)
+               : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, uint32_t lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(kFull, x, d);
+    if (lane >= (uint32_t)d) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long x,
+                                                               uint32_t lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long y = __shfl_up_sync(kFull, x, d);
+    if (lane >= (uint32_t)d) x += y;
+  }
+  return x;
+}
+
+// Last entry j in [0, F) with qp[j] <= x, for a non-decreasing qp with
+// qp[0] <= x: a 32-ary search, one probe per lane and round.
+__device__ __forceinline__ uint32_t warp_owner_search(const uint32_t *__restrict__ qp,
+                                                      uint32_t F, uint32_t x,
+                                                      uint32_t lane) {
+  uint32_t lo = 0, hi = F;  // qp[lo] <= x < qp[hi] (qp[F] = edge total)
+  while (hi - lo > 32u) {
+    const uint32_t step = (hi - lo + 31u) >> 5;
+    const uint32_t j = lo + lane * step;
+    const uint32_t val = (j < hi) ? qp[j] : kFull;
+    const uint32_t m = __ballot_sync(kFull, val <= x);
+    const uint32_t t = 31u - __clz(m);
+    lo = lo + t * step;
+    hi = min(hi, lo + step);
+  }
+  const uint32_t j = lo + lane;
+  const uint32_t val = (j < hi) ? qp[j] : kFull;
+  const uint32_t m = __ballot_sync(kFull, val <= x);
+  return lo + 31u - __clz(m);
+}
+
+}  // namespace bfsgb

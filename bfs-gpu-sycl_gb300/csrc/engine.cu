@@ -658,6 +658,7 @@ bfs_status bfs_graph_free(bfs_graph *g) {
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
   free_sched(g);
+  free_msbfs(g);
   free_workspace(g);
   if (g->owns_csc) {
     cudaFree(g->indptr);

@@ -34,9 +34,12 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts,
 // loop) instead of a grid sized to the frontier.
 cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32_t F,
                            uint32_t EF, bool persistent);
-void free_sched(bfs_graph *g);  // bfs_sched.cu
+void free_sched(bfs_graph *g);   // bfs_sched.cu
+void free_msbfs(bfs_graph *g);   // msbfs.cu
 
 }  // namespace bfsgb
+
+struct MsWorkspace;
 
 struct bfs_graph {
   int device = 0;
@@ -69,4 +72,5 @@ struct bfs_graph {
   int32_t host_arms[BFS_MAX_RECORDED_LEVELS] = {};
   uint32_t host_launches = 0;
   bfsgb::SchedModel *sched = nullptr;
+  MsWorkspace *ms = nullptr;  // multi-source BFS workspace (lazy)
 };

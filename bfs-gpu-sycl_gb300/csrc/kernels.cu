@@ -33,28 +33,10 @@
 #include <cstdint>
 
 #include "bfs_internal.h"
+#include "device_util.cuh"
 #include "kernels.h"
 
 namespace bfsgb {
-
-constexpr uint32_t kFull = 0xFFFFFFFFu;
-
-// ---- device helpers ---------------------------------------------------------
-
-// Edge-array load: read once per BFS, so bypass L1 and mark evict-first in L2
-// to keep the L2 for the visited bitmaps and queues.
-__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p, uint64_t pol) {
-  uint32_t r;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
-               : "=r"(r)
-               : "l"(p), "l"(pol));
-  return r;
-}
-__device__ __forceinline__ uint64_t evict_first_policy() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
 
 // Test-then-claim of bit n.  The plain load may see a stale 0 (L1 copy);
 // atomicOr's return value is authoritative, so exactly one thread claims n.
@@ -68,24 +50,6 @@ __device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent
   } else {
     atomicOr(vis + w, bit);  // result unused: a reduction, no round trip
   }
-}
-
-__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, uint32_t lane) {
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    uint32_t y = __shfl_up_sync(kFull, x, d);
-    if (lane >= (uint32_t)d) x += y;
-  }
-  return x;
-}
-__device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long x,
-                                                               uint32_t lane) {
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    unsigned long long y = __shfl_up_sync(kFull, x, d);
-    if (lane >= (uint32_t)d) x += y;
-  }
-  return x;
 }
 
 // Owner resolution for one warp round.  `cur` is an entry whose start is at
@@ -269,25 +233,6 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
 // (one probe per lane and round), then walks forward: each round loads the
 // next 32 entry starts and first-edge offsets coalesced, and every lane takes
 // its owner's offsets from those registers with shuffles.
-__device__ __forceinline__ uint32_t warp_owner_search(const uint32_t *__restrict__ qp,
-                                                      uint32_t F, uint32_t x,
-                                                      uint32_t lane) {
-  uint32_t lo = 0, hi = F;  // qp[lo] <= x < qp[hi] (qp[F] = edge total)
-  while (hi - lo > 32u) {
-    const uint32_t step = (hi - lo + 31u) >> 5;
-    const uint32_t j = lo + lane * step;
-    const uint32_t val = (j < hi) ? qp[j] : kFull;
-    const uint32_t m = __ballot_sync(kFull, val <= x);
-    const uint32_t t = 31u - __clz(m);
-    lo = lo + t * step;
-    hi = min(hi, lo + step);
-  }
-  const uint32_t j = lo + lane;
-  const uint32_t val = (j < hi) ? qp[j] : kFull;
-  const uint32_t m = __ballot_sync(kFull, val <= x);
-  return lo + 31u - __clz(m);
-}
-
 template <int B, int U>
 __global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;

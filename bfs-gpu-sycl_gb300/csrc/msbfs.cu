@@ -1,0 +1,496 @@
+// msbfs.cu -- batched multi-source BFS, 64 roots per uint64 lane.
+//
+// The reference runs one root per invocation (src/host.cpp:72, :146-150) and
+// re-uploads the graph every run (src/run_bfs_gpu.hpp:620-670).  Here up to 64
+// roots share every level: each vertex carries a 64-bit visited mask (bit j =
+// reached by root j) and the frontier queue carries, per entry, the mask of
+// roots whose frontier contains it.  One traversal of an edge u->v serves every
+// root whose frontier holds u:  next[v] |= mask(u) & ~visited[v].
+// Level generation turns next[] into the new frontier, writes each root's
+// int32 level row and each root's edgesCount (sum of degrees of the vertices
+// that root expands, run_bfs_cpu.hpp:36), so every row is exactly the
+// single-root level array of its root.
+//
+//   explore   edge-balanced like the GLB form: a warp takes a chunk of the
+//             frontier's edges, finds the owner of its first edge with a 32-ary
+//             search of the degree prefix, then takes each owner's first edge
+//             and root mask from shuffles of coalesced loads.
+//   levelgen  one vertex per lane: new = next[v] & ~visited[v]; the warp
+//             iterates over the union of new bits, storing level[j][v] for the
+//             lanes holding bit j (coalesced per root row) and reducing those
+//             lanes' degrees into root j's edge counter; kept vertices are
+//             compacted with ballot/popc and one atomic per block.
+//   loop      a CUDA graph with a conditional WHILE node, as for one root.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bfs_internal.h"
+#include "device_util.cuh"
+#include "engine.h"
+#include "kernels.h"
+
+namespace bfsgb {
+
+constexpr int kLanes = 64;
+constexpr int kMsBlock = 256;
+constexpr int kMsU = 4;
+constexpr uint32_t kMsChunk = 32u * kMsU * 4u;
+
+struct MsState {
+  const uint32_t *indptr;
+  const uint32_t *inds;
+  uint32_t n_rows, n_cols;
+  unsigned long long *vis;
+  unsigned long long *next;
+  uint32_t *qb[2];
+  uint32_t *qp[2];
+  unsigned long long *qm[2];
+  int32_t *level;  // n_lanes rows of n_cols
+  uint32_t n_lanes;
+  uint32_t roots[kLanes];
+  unsigned long long next_packed;
+  uint32_t cur, F, EF, lvl;
+  uint32_t done_blocks, error, level_cap, max_level, any_new;
+  uint32_t launches;
+  unsigned long long edges[kLanes];
+};
+
+__global__ void ms_fill_kernel(MsState *st) {
+  int32_t *level = st->level;
+  const uint64_t total = (uint64_t)st->n_lanes * st->n_cols;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const bool vec = (reinterpret_cast<uintptr_t>(level) & 15u) == 0;
+  const uint64_t n4 = vec ? total / 4 : 0;
+  const int4 neg = make_int4(-1, -1, -1, -1);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
+    reinterpret_cast<int4 *>(level)[i] = neg;
+  for (uint64_t i = n4 * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += stride)
+    level[i] = -1;
+}
+
+// One block of 64 threads: seeds every root and builds the first frontier
+// (roots shared by several lanes become one entry with several mask bits).
+__global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_cond) {
+  const uint32_t j = threadIdx.x;
+  const uint32_t n = st->n_cols;
+  if (j < st->n_lanes) {
+    const uint32_t r = st->roots[j];
+    st->level[(size_t)j * n + r] = 0;
+    atomicOr(&st->vis[r], 1ull << j);
+    st->edges[j] = r < st->n_rows ? (unsigned long long)(st->indptr[r + 1] - st->indptr[r]) : 0ull;
+  } else if (j < kLanes) {
+    st->edges[j] = 0;
+  }
+  __syncthreads();
+  if (j == 0) {
+    uint32_t F = 0, EF = 0;
+    for (uint32_t l = 0; l < st->n_lanes; l++) {
+      const uint32_t r = st->roots[l];
+      if (r >= st->n_rows) continue;
+      const uint32_t b = st->indptr[r], e = st->indptr[r + 1];
+      if (e == b) continue;
+      uint32_t k = 0;
+      while (k < F && st->qb[0][k] != b) k++;  // same root -> same first edge
+      if (k < F) {
+        st->qm[0][k] |= 1ull << l;
+        continue;
+      }
+      st->qb[0][F] = b;
+      st->qp[0][F] = EF;
+      st->qm[0][F] = 1ull << l;
+      EF += e - b;
+      F++;
+    }
+    st->qp[0][F] = EF;
+    st->F = F;
+    st->EF = EF;
+    st->cur = 0;
+    st->lvl = 0;
+    st->next_packed = 0;
+    st->done_blocks = 0;
+    st->error = 0;
+    st->max_level = 0;
+    st->any_new = 0;
+    st->launches = 3;
+    if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, F > 0);
+  }
+}
+
+__global__ void __launch_bounds__(kMsBlock) ms_explore_kernel(MsState *__restrict__ st) {
+  constexpr int NW = kMsBlock / 32;
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  const uint32_t EF = st->EF;
+  const uint32_t cq = st->cur;
+  const uint32_t *__restrict__ qb = st->qb[cq];
+  const uint32_t *__restrict__ qp = st->qp[cq];
+  const unsigned long long *__restrict__ qm = st->qm[cq];
+  const uint32_t *__restrict__ inds = st->inds;
+  const unsigned long long *vis = st->vis;
+  unsigned long long *next = st->next;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint64_t pol = evict_first_policy();
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + kMsChunk - 1) / kMsChunk);
+  const uint32_t total_warps = gridDim.x * NW;
+
+  for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
+    const uint32_t w0 = c * kMsChunk;
+    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + kMsChunk);
+    uint32_t cur = warp_owner_search(qp, F, w0, lane);
+    uint32_t cur_start = qp[cur], cur_beg = qb[cur];
+    unsigned long long cur_mask = qm[cur];
+    for (uint32_t base = w0; base < w1; base += 32u * kMsU) {
+      uint32_t addr[kMsU];
+      unsigned long long msk[kMsU];
+#pragma unroll
+      for (int u = 0; u < kMsU; u++) {
+        const uint32_t rb = base + 32u * u;
+        const uint32_t e = rb + lane;
+        const uint32_t j = cur + 1u + lane;
+        const uint32_t bnd = (j <= F) ? qp[j] : kFull;
+        const uint32_t bg = (j < F) ? qb[j] : 0u;
+        const unsigned long long mk = (j < F) ? qm[j] : 0ull;
+        const uint32_t p = bnd - rb;
+        const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
+        const uint32_t k = __popc(starts & ((2u << lane) - 1u));
+        const uint32_t srcl = k ? k - 1u : 0u;
+        const uint32_t s_start = __shfl_sync(kFull, bnd, srcl);
+        const uint32_t s_beg = __shfl_sync(kFull, bg, srcl);
+        const unsigned long long s_mask = __shfl_sync(kFull, mk, srcl);
+        addr[u] = kFull;
+        msk[u] = 0;
+        if (e < w1) {
+          addr[u] = (k ? s_beg : cur_beg) + (e - (k ? s_start : cur_start));
+          msk[u] = k ? s_mask : cur_mask;
+        }
+        const uint32_t k31 = __shfl_sync(kFull, k, 31);
+        if (k31) {
+          cur += k31;
+          cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
+          cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
+          cur_mask = __shfl_sync(kFull, mk, k31 - 1u);
+        }
+      }
+      uint32_t nb[kMsU];
+#pragma unroll
+      for (int u = 0; u < kMsU; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
+#pragma unroll
+      for (int u = 0; u < kMsU; u++) {
+        if (addr[u] == kFull) continue;
+        const unsigned long long bits = msk[u] & ~vis[nb[u]];
+        if (bits) atomicOr(next + nb[u], bits);
+      }
+    }
+  }
+}
+
+__device__ void ms_finish(MsState *st, unsigned long long cond, int use_cond) {
+  const unsigned long long packed = *(volatile unsigned long long *)&st->next_packed;
+  const uint32_t f_new = (uint32_t)(packed >> 32), ef_new = (uint32_t)packed;
+  const uint32_t lvl = st->lvl + 1;
+  if (*(volatile uint32_t *)&st->any_new) st->max_level = lvl;
+  st->any_new = 0;
+  const uint32_t nq = st->cur ^ 1u;
+  st->qp[nq][f_new] = ef_new;
+  st->cur = nq;
+  st->F = f_new;
+  st->EF = ef_new;
+  st->lvl = lvl;
+  st->next_packed = 0;
+  st->done_blocks = 0;
+  st->launches += 2;
+  if (f_new > 0 && lvl >= st->level_cap) {
+    st->error |= BFS_DEVERR_LEVEL_LIMIT;
+    st->F = 0;
+  }
+  if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
+}
+
+__global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restrict__ st,
+                                                               unsigned long long cond,
+                                                               int use_cond) {
+  constexpr int NW = kMsBlock / 32;
+  __shared__ unsigned long long s_edges[kLanes];
+  __shared__ unsigned long long s_wtot[NW];
+  __shared__ unsigned long long s_base;
+  __shared__ int s_last;
+  __shared__ uint32_t s_any;
+  const uint32_t n_cols = st->n_cols, n_rows = st->n_rows;
+  unsigned long long *__restrict__ vis = st->vis;
+  unsigned long long *__restrict__ next = st->next;
+  const uint32_t *__restrict__ indptr = st->indptr;
+  int32_t *__restrict__ level = st->level;
+  const int32_t lvl_next = (int32_t)st->lvl + 1;
+  const uint32_t nq = st->cur ^ 1u;
+  uint32_t *__restrict__ qb = st->qb[nq];
+  uint32_t *__restrict__ qp = st->qp[nq];
+  unsigned long long *__restrict__ qm = st->qm[nq];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  if (threadIdx.x < kLanes) s_edges[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  bool any = false;
+  const uint64_t span = (uint64_t)kMsBlock;
+  for (uint64_t sb = (uint64_t)blockIdx.x * span; sb < n_cols; sb += (uint64_t)gridDim.x * span) {
+    const uint32_t v = (uint32_t)(sb + threadIdx.x);
+    unsigned long long nw = 0;
+    uint32_t b = 0, e = 0;
+    if (v < n_cols) {
+      const unsigned long long nx = next[v];
+      if (nx) {
+        next[v] = 0;
+        const unsigned long long vv = vis[v];
+        nw = nx & ~vv;
+        if (nw) {
+          vis[v] = vv | nw;
+          if (v < n_rows) {
+            b = indptr[v];
+            e = indptr[v + 1];
+          }
+        }
+      }
+    }
+    any |= nw != 0;
+    const uint32_t deg = e - b;
+    // levels and per-root edge counts, one root row at a time
+    const uint32_t u_lo = __reduce_or_sync(kFull, (uint32_t)nw);
+    const uint32_t u_hi = __reduce_or_sync(kFull, (uint32_t)(nw >> 32));
+    for (uint32_t m = u_lo; m; m &= m - 1u) {
+      const uint32_t j = __ffs(m) - 1u;
+      const bool has = (nw >> j) & 1ull;
+      if (has) level[(size_t)j * n_cols + v] = lvl_next;
+      const uint32_t ds = __reduce_add_sync(kFull, has ? deg : 0u);
+      if (lane == 0 && ds) atomicAdd(&s_edges[j], (unsigned long long)ds);
+    }
+    for (uint32_t m = u_hi; m; m &= m - 1u) {
+      const uint32_t j = 32u + __ffs(m) - 1u;
+      const bool has = (nw >> j) & 1ull;
+      if (has) level[(size_t)j * n_cols + v] = lvl_next;
+      const uint32_t ds = __reduce_add_sync(kFull, has ? deg : 0u);
+      if (lane == 0 && ds) atomicAdd(&s_edges[j], (unsigned long long)ds);
+    }
+    // compact the kept vertices: ballot/popc per warp, one atomic per block
+    const uint32_t km = __ballot_sync(kFull, deg > 0u);
+    const uint32_t dincl = warp_incl_scan(deg, lane);
+    if (lane == 31) s_wtot[warp] = ((unsigned long long)__popc(km) << 32) | dincl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long run = 0;
+      for (int i = 0; i < NW; i++) {
+        const unsigned long long t = s_wtot[i];
+        s_wtot[i] = run;
+        run += t;
+      }
+      s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
+    }
+    __syncthreads();
+    if (deg) {
+      const unsigned long long wb = s_base + s_wtot[warp];
+      const uint32_t slot = (uint32_t)(wb >> 32) + __popc(km & lt_mask);
+      qb[slot] = b;
+      qp[slot] = (uint32_t)wb + dincl - deg;
+      qm[slot] = nw;
+    }
+    __syncthreads();
+  }
+  if (any) s_any = 1;
+  __syncthreads();
+  if (threadIdx.x < kLanes && s_edges[threadIdx.x])
+    atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x]);
+  if (threadIdx.x == 0) {
+    if (s_any) atomicOr(&st->any_new, 1u);
+    __threadfence();
+    const uint32_t ticket = atomicAdd(&st->done_blocks, 1u);
+    s_last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    ms_finish(st, cond, use_cond);
+  }
+}
+
+}  // namespace bfsgb
+
+// ---- host side ----------------------------------------------------------------
+using namespace bfsgb;
+
+struct MsWorkspace {
+  void *mem = nullptr;
+  MsState *d_st = nullptr;
+  MsState *h_st = nullptr;  // pinned
+  MsState tmpl{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int grid_ex = 0, grid_lg = 0, grid_fill = 0;
+};
+
+namespace bfsgb {
+
+void free_msbfs(bfs_graph *g) {
+  MsWorkspace *w = g->ms;
+  if (!w) return;
+  if (w->exec) cudaGraphExecDestroy(w->exec);
+  if (w->graph) cudaGraphDestroy(w->graph);
+  if (w->e0) cudaEventDestroy(w->e0);
+  if (w->e1) cudaEventDestroy(w->e1);
+  cudaFree(w->mem);
+  cudaFree(w->d_st);
+  if (w->h_st) cudaFreeHost(w->h_st);
+  delete w;
+  g->ms = nullptr;
+}
+
+}  // namespace bfsgb
+
+#define MK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(e_ == cudaErrorMemoryAllocation ? BFS_ERR_OOM : BFS_ERR_CUDA,    \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+static bfs_status ms_setup(bfs_graph *g) {
+  if (g->ms) return BFS_OK;
+  MsWorkspace *w = new MsWorkspace();
+  g->ms = w;
+  const size_t n = g->n_cols, nr = std::max<uint32_t>(g->n_rows, 1);
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t b64 = al(n * 8), q4 = al(nr * 4), qp4 = al((nr + 1) * 4), q8 = al(nr * 8);
+  const size_t bytes = 2 * b64 + 2 * (q4 + qp4 + q8);
+  MK(cudaMalloc(&w->mem, bytes));
+  MK(cudaMalloc(&w->d_st, sizeof(MsState)));
+  MK(cudaMallocHost(&w->h_st, sizeof(MsState)));
+  MK(cudaEventCreate(&w->e0));
+  MK(cudaEventCreate(&w->e1));
+  char *p = (char *)w->mem;
+  MsState &s = w->tmpl;
+  std::memset(&s, 0, sizeof(s));
+  s.indptr = g->indptr;
+  s.inds = g->inds;
+  s.n_rows = g->n_rows;
+  s.n_cols = g->n_cols;
+  s.vis = (unsigned long long *)p; p += b64;
+  s.next = (unsigned long long *)p; p += b64;
+  for (int b = 0; b < 2; b++) {
+    s.qb[b] = (uint32_t *)p; p += q4;
+    s.qp[b] = (uint32_t *)p; p += qp4;
+    s.qm[b] = (unsigned long long *)p; p += q8;
+  }
+  s.level_cap = g->n_cols + 1u;
+  int occ_ex = 0, occ_lg = 0;
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, (const void *)ms_explore_kernel,
+                                                   kMsBlock, 0));
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, (const void *)ms_levelgen_kernel,
+                                                   kMsBlock, 0));
+  w->grid_ex = g->num_sms * std::max(occ_ex, 1);
+  w->grid_lg = g->num_sms * std::max(occ_lg, 1);
+  w->grid_fill = g->num_sms * 8;
+
+  // graph: memset(vis, next) -> fill -> init -> while(F > 0) { explore -> levelgen }
+  MK(cudaGraphCreate(&w->graph, 0));
+  cudaGraphConditionalHandle cond;
+  MK(cudaGraphConditionalHandleCreate(&cond, w->graph, 0, cudaGraphCondAssignDefault));
+  unsigned long long cond_arg = (unsigned long long)cond;
+  int one = 1;
+  MsState *st = w->d_st;
+  cudaMemsetParams mp;
+  std::memset(&mp, 0, sizeof(mp));
+  mp.dst = w->mem;
+  mp.elementSize = 4;
+  mp.width = 2 * b64 / 4;
+  mp.height = 1;
+  cudaGraphNode_t n_ms, n_fill, n_init, n_while, n_ex, n_lg;
+  MK(cudaGraphAddMemsetNode(&n_ms, w->graph, nullptr, 0, &mp));
+  cudaKernelNodeParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  void *fill_args[] = {&st};
+  kp.func = (void *)ms_fill_kernel;
+  kp.gridDim = dim3(w->grid_fill);
+  kp.blockDim = dim3(256);
+  kp.kernelParams = fill_args;
+  MK(cudaGraphAddKernelNode(&n_fill, w->graph, &n_ms, 1, &kp));
+  void *init_args[] = {&st, &cond_arg, &one};
+  kp.func = (void *)ms_init_kernel;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(kLanes);
+  kp.kernelParams = init_args;
+  MK(cudaGraphAddKernelNode(&n_init, w->graph, &n_fill, 1, &kp));
+  alignas(cudaGraphNodeParams) unsigned char wbuf[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams &wp = *reinterpret_cast<cudaGraphNodeParams *>(wbuf);
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = cond;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  MK(cudaGraphAddNode(&n_while, w->graph, &n_init, nullptr, 1, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  void *ex_args[] = {&st};
+  kp.func = (void *)ms_explore_kernel;
+  kp.gridDim = dim3(w->grid_ex);
+  kp.blockDim = dim3(kMsBlock);
+  kp.kernelParams = ex_args;
+  MK(cudaGraphAddKernelNode(&n_ex, body, nullptr, 0, &kp));
+  void *lg_args[] = {&st, &cond_arg, &one};
+  kp.func = (void *)ms_levelgen_kernel;
+  kp.gridDim = dim3(w->grid_lg);
+  kp.blockDim = dim3(kMsBlock);
+  kp.kernelParams = lg_args;
+  MK(cudaGraphAddKernelNode(&n_lg, body, &n_ex, 1, &kp));
+  MK(cudaGraphInstantiate(&w->exec, w->graph, 0));
+  return BFS_OK;
+}
+
+extern "C" bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                                    int32_t *levels_dev, uint64_t *edges_count_out,
+                                    bfs_batch_stats *stats) {
+  if (!g || !roots || !levels_dev) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  for (uint32_t i = 0; i < n_roots; i++)
+    if (roots[i] >= g->n_cols) return fail(BFS_ERR_ROOT, "root out of range");
+  MK(cudaSetDevice(g->device));
+  bfs_status rc = ms_setup(g);
+  if (rc != BFS_OK) {
+    free_msbfs(g);
+    return rc;
+  }
+  MsWorkspace *w = g->ms;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  double total_ms = 0.0;
+  for (uint32_t b0 = 0; b0 < n_roots; b0 += kLanes) {
+    const uint32_t nl = std::min<uint32_t>(kLanes, n_roots - b0);
+    MsState &s = *w->h_st;
+    s = w->tmpl;
+    s.level = levels_dev + (size_t)b0 * g->n_cols;
+    s.n_lanes = nl;
+    for (uint32_t j = 0; j < nl; j++) s.roots[j] = roots[b0 + j];
+    MK(cudaEventRecord(w->e0, g->stream));
+    MK(cudaMemcpyAsync(w->d_st, w->h_st, sizeof(MsState), cudaMemcpyHostToDevice, g->stream));
+    MK(cudaGraphLaunch(w->exec, g->stream));
+    MK(cudaEventRecord(w->e1, g->stream));
+    MK(cudaMemcpyAsync(w->h_st, w->d_st, sizeof(MsState), cudaMemcpyDeviceToHost, g->stream));
+    MK(cudaStreamSynchronize(g->stream));
+    const MsState &r = *w->h_st;
+    if (r.error & BFS_DEVERR_LEVEL_LIMIT)
+      return fail(BFS_ERR_LEVEL_LIMIT, "level loop exceeded n_cols + 1 levels");
+    if (r.error) return fail(BFS_ERR_DEVICE, "device error flag " + std::to_string(r.error));
+    float ms = 0.f;
+    MK(cudaEventElapsedTime(&ms, w->e0, w->e1));
+    total_ms += ms;
+    if (edges_count_out)
+      for (uint32_t j = 0; j < nl; j++) edges_count_out[b0 + j] = r.edges[j];
+    if (stats) {
+      stats->batches++;
+      stats->max_levels = std::max(stats->max_levels, r.max_level + 1);
+      stats->launches += r.launches + 1;
+    }
+  }
+  if (stats) stats->device_ms = total_ms;
+  return BFS_OK;
+}

@@ -147,6 +147,23 @@ bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,
 bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,
                                const int32_t *parents_dev, uint64_t *bad);
 
+/* ---- batched multi-source BFS ------------------------------------------ */
+/* n_roots independent BFS runs on one graph, 64 roots per pass: each vertex
+ * carries a 64-bit visited mask and one traversal of an edge serves every
+ * root whose frontier holds its source.  Row i of levels_dev (n_roots x
+ * n_cols int32, device) is exactly the level array of roots[i];
+ * edges_count_out[i] (optional, host) its edgesCount.  The reference has one
+ * root per invocation (src/host.cpp:72). */
+typedef struct bfs_batch_stats {
+  double device_ms;       /* CUDA-event time of all passes */
+  uint32_t batches;       /* passes of up to 64 roots */
+  uint32_t max_levels;    /* deepest level + 1 over all roots */
+  uint32_t launches;      /* kernels launched */
+} bfs_batch_stats;
+bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                         int32_t *levels_dev, uint64_t *edges_count_out,
+                         bfs_batch_stats *stats);
+
 /* ---- BFS without device allocation ------------------------------------ */
 /* No counterpart in the reference (its GPURun allocates per run).  For
  * callers that cannot allocate device memory -- code inside an allocator or

@@ -1,19 +1,25 @@
 #!/usr/bin/env python
 """Benchmark: GTEPS of single-root top-down BFS on R-MAT scale 25, edge factor
 16 (seed 5, a/b/c/d = .57/.19/.19/.05, deduplicated, symmetrised, uint32 CSC),
-on one GB300.
+on one GB300, with the learned per-level schedule; fixed LLB beside it; and
+roots/s of 64-root batched BFS.
 
 One step = one BFS from one seeded root (degree > 0), the unit the reference
 times per run (src/run_bfs_gpu.hpp:679-728).  GTEPS = edgesCount / BFS time
 (src/host.cpp:196), edgesCount = sum of out-degrees of expanded vertices.
 
   value     device time (CUDA events on the engine's stream) of the whole BFS
-            with the graph resident in HBM: level init, every level, no copies
+            with the graph resident in HBM: level init, every level, no copies;
+            explore arm picked per level by the learned scheduler
   e2e       the same metric through the public C call bfs_run with a pinned
             host output buffer: root in, the n-entry int32 level array copied
             back inside the timed region, wall clock
-  roofline  the explore kernel (dominant): algorithmic bytes 4*E + 8*F per
-            launch (edges + frontier {beg,end} entries) / its CUDA-event time
+  roofline  the explore kernels (dominant): algorithmic bytes 4*E + 8*F per
+            launch (edges + frontier {beg, prefix} entries) / their CUDA-event
+            time, from a host-loop pass with per-kernel events
+  fixed_llb the same workload with the fixed LLB/256 explore (the reference's
+            default build, src/CMakeLists.txt:10-11)
+  batched   64 roots per bfs_run_batch pass vs 64 sequential single-root runs
   cpu_baseline  the oracle (C restatement of run_bfs_cpu) on one root of the
             same graph, one host thread
 
@@ -38,7 +44,8 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "GTEPS at RMAT-25/EF16 on 1xGB300 (single-root top-down BFS)"
+METRIC = "GTEPS at RMAT-25/EF16 on 1xGB300: learned-schedule vs fixed-LLB; roots/s batched"
+WEIGHTS = os.path.join(PKG, "sched_weights.f32")
 UNIT = "GTEPS"
 
 
@@ -51,7 +58,10 @@ def parse():
     ap.add_argument("--scale", type=int, default=25)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=5)
-    ap.add_argument("--lb", default="llb", help="explore plan for `value`")
+    ap.add_argument("--lb", default="learned", help="explore plan for `value`")
+    ap.add_argument("--loop", default="graph", choices=["graph", "host"],
+                    help="level-loop driver (host: every kernel a plain launch, for ncu)")
+    ap.add_argument("--skip-batched", action="store_true", help="omit the batched leg")
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-arms", action="store_true", help="omit the per-arm table")
@@ -179,7 +189,11 @@ def run_gb300(a):
     host = dg.download()
     roots = B.sample_roots(host, a.warmup + a.steps + 8, a.seed + 1000 * rank)
     lv = torch.empty(n, dtype=torch.int32, device="cuda")
-    opts = B.options(a.lb, a.block)
+    weights = None
+    if os.path.exists(WEIGHTS):
+        weights = np.fromfile(WEIGHTS, dtype="<f4")
+        dg.sched_attach(weights)
+    opts = B.options(a.lb, a.block, loop=a.loop)
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -228,6 +242,16 @@ def run_gb300(a):
     (e_wall_max,), (e_edges_sum,) = reduce_max_sum([e_wall], [e_edges], world)
     e2e = e_edges_sum / e_wall_max / 1e9
 
+    # fixed LLB/256 on the same roots (the reference's default build)
+    llb_ms, llb_edges = 0.0, 0.0
+    o_llb = B.options("llb", 256, loop=a.loop)
+    dg.run_device(int(roots[0]), lv.data_ptr(), opts=o_llb)
+    for r in roots[a.warmup:a.warmup + a.steps]:
+        st = dg.run_device(int(r), lv.data_ptr(), opts=o_llb)
+        llb_ms += st.device_ms
+        llb_edges += st.edges_count
+    llb_gteps = llb_edges / (llb_ms * 1e-3) / 1e9
+
     # explore-kernel roofline: per-level CUDA-event times in the host loop
     prof_bytes, prof_ms, gen_ms, lvl_rows = 0.0, 0.0, 0.0, []
     for r in roots[a.warmup:a.warmup + 3]:
@@ -242,8 +266,8 @@ def run_gb300(a):
             prof_ms += tab["explore_ms"][i]
             gen_ms += tab["gen_ms"][i]
             if r == roots[a.warmup]:
-                lvl_rows.append([i, F, EF, round(tab["explore_ms"][i], 4),
-                                 round(tab["gen_ms"][i], 4)])
+                lvl_rows.append([i, F, EF, B.ARM_NAMES[tab["arm"][i]],
+                                 round(tab["explore_ms"][i], 4), round(tab["gen_ms"][i], 4)])
     achieved = prof_bytes / (prof_ms * 1e-3) / 1e9 if prof_ms > 0 else None
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "explore_traffic.json")
@@ -267,6 +291,34 @@ def run_gb300(a):
                     ed += st.edges_count
                 arms[f"{lb}{blk}"] = round(ed / (ms * 1e-3) / 1e9, 3)
 
+    # batched: one 64-root multi-source pass vs 64 sequential runs
+    batched = None
+    if not a.skip_batched:
+        broots = roots[:64] if len(roots) >= 64 else B.sample_roots(host, 64, a.seed + 7)
+        if len(broots) < 64:
+            broots = B.sample_roots(host, 64, a.seed + 7)
+        out = torch.empty((64, n), dtype=torch.int32, device="cuda")
+        dg.run_batch(broots, out.data_ptr(), want_edges=False)
+        bms = []
+        for _ in range(3):
+            _, bst = dg.run_batch(broots, out.data_ptr(), want_edges=False)
+            bms.append(bst.device_ms)
+        b_ms = min(bms)
+        seq = {}
+        for name, o in (("llb256", B.options("llb", 256)), ("learned", opts)):
+            seq[name] = sum(dg.run_device(int(r), lv.data_ptr(), opts=o).device_ms
+                            for r in broots)
+        del out
+        batched = {"roots_per_s": round(64 / (b_ms * 1e-3), 1),
+                   "batch64_ms": round(b_ms, 3),
+                   "sequential_llb256_roots_per_s": round(64 / (seq["llb256"] * 1e-3), 1),
+                   "sequential_learned_roots_per_s": round(64 / (seq["learned"] * 1e-3), 1),
+                   "speedup_vs_sequential_llb256": round(seq["llb256"] / b_ms, 2),
+                   "speedup_vs_sequential_learned": round(seq["learned"] / b_ms, 2),
+                   "levels": bst.max_levels,
+                   "workload": f"64 seeded roots on the same RMAT-{a.scale} graph, device "
+                               "CUDA-event time of one bfs_run_batch pass vs 64 bfs_run_device"}
+
     # CPU baseline: the oracle on one root, one thread (rank 0 only)
     cpu = None
     if rank == 0 and not a.skip_cpu:
@@ -282,6 +334,7 @@ def run_gb300(a):
                f"graph, level-synchronous run_bfs_cpu restatement, {cpu_s:.2f} s",
                "parity_with_gpu": match}
 
+    plan = "learned per-level schedule" if a.lb == "learned" else f"{a.lb}{a.block}"
     mean_edges = tot_edges / len(edges)
     mean_reached = sum(reached) / len(reached)
     bfs_gbs = bfs_bytes(mean_edges, mean_reached, n) / ((total_ms / len(dev_ms)) * 1e-3) / 1e9
@@ -292,7 +345,9 @@ def run_gb300(a):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded R-MAT generated on the device)",
         "config": {"workload": f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, single-root "
-                   f"BFS, explore plan {a.lb}{a.block}, device CUDA-graph level loop",
+                   f"BFS, explore plan {plan}, {a.loop} level loop",
+                   "scheduler_weights": os.path.basename(WEIGHTS) if weights is not None
+                   else None,
                    "vertices": n, "edges": dg.nnz, "roots_timed": a.steps,
                    "l2": "inputs larger than L2 (4 B x edges >> 129 MB)",
                    "graph_gen_s": round(gen_s, 2), "timed_wall_s": round(wall, 4)},
@@ -310,6 +365,9 @@ def run_gb300(a):
         "clocks": clocks,
         "gpu_launches": launches,
         "validator_violations": int(bad),
+        "fixed_llb256": {"value": round(llb_gteps, 4), "unit": UNIT},
+        "learned_vs_fixed_llb256": round(value / llb_gteps, 3) if a.lb == "learned" else None,
+        "batched": batched,
         "arms_gteps": arms,
         "levels_first_root": lvl_rows,
     }

@@ -731,4 +731,14 @@ bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *level
   return BFS_OK;
 }
 
+bfs_status bfs_validate_host(bfs_graph *g, uint32_t root, const int32_t *levels_host,
+                             uint64_t *bad) {
+  if (!g || !levels_host || !bad) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  CK(cudaSetDevice(g->device));
+  const size_t bytes = sizeof(int32_t) * (size_t)g->n_cols;
+  if (!g->d_out_levels) CK(cudaMalloc(&g->d_out_levels, bytes));
+  CK(cudaMemcpy(g->d_out_levels, levels_host, bytes, cudaMemcpyHostToDevice));
+  return bfs_validate_device(g, root, g->d_out_levels, nullptr, bad);
+}
+
 }  // extern "C"

@@ -1,0 +1,264 @@
+// bfs_main.cpp -- command line driver with the reference's surface.
+//
+// Mirrors the reference's `bfs_<N>.gpu` program (src/host.cpp:57-276):
+//   --num_runs (1) --dataset (default) --root (1) --output (data.json)
+// parsed like CommandLineParser (src/functions.hpp:7-61): "--key=value" or
+// "--key value", unknown keys ignored, a missing value only warns.  It loads
+// $PWD/dataset/<dataset>-csc-<P>/ (src/graph_load.hpp:93-132), runs GPURun
+// num_runs times from the root, and merges one JSON object into the output
+// file under [<dataset>_<num_runs>_<variant>][<P>] (host.cpp:228-271) with the
+// reference's keys.
+//
+// Extra flags (the reference fixes these at compile time,
+// src/CMakeLists.txt:6-12):
+//   --partitions P   dataset partition count (the reference's NUM_GPU); the
+//                    partitions are merged and run on one GPU
+//   --lb llb|glb|slb|learned   explore form (default llb, or the build macro)
+//   --block 128|256|512  --ipt 4|8  --loop graph|host
+//   --weights FILE   scheduler weights for --lb learned
+//                    (default: sched_weights.f32 of the package)
+//   --dataset_dir DIR   instead of $PWD/dataset
+// Validation: the reference compares the last GPU run with its CPU BFS
+// (host.cpp:184-188).  This driver keeps the cross-run comparison
+// (functions.hpp:131-163) and replaces the CPU run with the device's exact
+// level check (root at 0, every edge within one level, every reached vertex
+// with a parent one level up), so `valid` means the same thing.
+// Corrected reference quirks (values are the reference's formulas without
+// them): edgesCount is not truncated to 32 bits (host.cpp:194-202) and
+// edgesCoverage is a real percentage (host.cpp:203 divides integers).
+#include <unistd.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "bfs_gb300.h"
+#include "bfs_gpurun.hpp"
+#include "bfs_json.hpp"
+
+namespace {
+
+class ArgParser {
+ public:
+  void add(const std::string &k, const std::string &v) { args_[k] = v; }
+  void parse(int argc, char **argv) {
+    for (int i = 1; i < argc; ++i) {
+      std::string a = argv[i];
+      if (a.rfind("--", 0) != 0) continue;
+      const size_t eq = a.find('=');
+      if (eq != std::string::npos) {
+        const std::string k = a.substr(2, eq - 2);
+        if (args_.count(k)) args_[k] = a.substr(eq + 1);
+      } else if (i + 1 < argc && argv[i + 1][0] != '-') {
+        const std::string k = a.substr(2);
+        const std::string v = argv[++i];
+        if (args_.count(k)) args_[k] = v;
+      } else {
+        std::cerr << "Warning: No value provided for argument " << a << std::endl;
+      }
+    }
+  }
+  const std::string &get(const std::string &k) const { return args_.at(k); }
+  void print() const {
+    for (const auto &kv : args_)
+      std::cout << std::setw(20) << std::left << "- " + kv.first << std::setw(20) << kv.second
+                << std::endl;
+  }
+
+ private:
+  std::map<std::string, std::string> args_;
+};
+
+std::string exe_dir() {
+  char buf[PATH_MAX];
+  ssize_t n = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+  if (n <= 0) return ".";
+  buf[n] = 0;
+  std::string p(buf);
+  return p.substr(0, p.rfind('/'));
+}
+
+int lb_from_name(const std::string &s) {
+  if (s == "llb" || s == "local") return BFS_LB_LLB;
+  if (s == "glb" || s == "global") return BFS_LB_GLB;
+  if (s == "slb" || s == "local_strided") return BFS_LB_SLB;
+  if (s == "learned") return BFS_LB_LEARNED;
+  return -2;
+}
+
+const char *variant_key(int lb) {
+  switch (lb) {
+    case BFS_LB_GLB: return "global";
+    case BFS_LB_SLB: return "local_strided";
+    case BFS_LB_LEARNED: return "learned";
+    default: return "local";
+  }
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  ArgParser parser;
+  parser.add("num_runs", "1");
+  parser.add("dataset", "default");
+  parser.add("root", "1");
+  parser.add("output", "data.json");
+  parser.add("partitions", "1");
+  parser.add("lb", variant_key(bfs::default_lb()) == std::string("global")
+                       ? "glb"
+                       : (bfs::default_lb() == BFS_LB_SLB ? "slb" : "llb"));
+  parser.add("block", "256");
+  parser.add("ipt", "4");
+  parser.add("loop", "graph");
+  parser.add("weights", exe_dir() + "/../sched_weights.f32");
+  parser.add("dataset_dir", "");
+  parser.parse(argc, argv);
+
+  int num_runs, start_vertex, parts, block, ipt;
+  try {
+    num_runs = std::stoi(parser.get("num_runs"));
+    start_vertex = std::stoi(parser.get("root"));
+    parts = std::stoi(parser.get("partitions"));
+    block = std::stoi(parser.get("block"));
+    ipt = std::stoi(parser.get("ipt"));
+  } catch (const std::exception &e) {
+    std::cerr << "ERROR: bad numeric argument (" << e.what() << ")" << std::endl;
+    return 1;
+  }
+  const std::string dataset = parser.get("dataset");
+  const std::string output = parser.get("output");
+  const int lb = lb_from_name(parser.get("lb"));
+  if (lb < -1 || num_runs < 1 || parts < 1 || start_vertex < 0) {
+    std::cerr << "ERROR: invalid --lb, --num_runs, --partitions or --root" << std::endl;
+    return 1;
+  }
+  parser.print();
+  std::cout << std::setw(20) << std::left << "- num_gpu" << std::setw(20) << 1 << std::endl;
+
+  bfs_csc_host g{};
+  const std::string dir = parser.get("dataset_dir");
+  bfs_status s = bfs_dataset_load(dir.empty() ? nullptr : dir.c_str(), dataset.c_str(),
+                                  (uint32_t)parts, &g);
+  if (s != BFS_OK) {
+    std::cerr << "ERROR: " << bfs_last_error() << std::endl;
+    return 1;
+  }
+  const uint32_t numRows = g.n_rows, numCols = g.n_cols;
+  const uint64_t numEdges = g.nnz;
+  std::cout << std::setw(20) << std::left << "- # vertices" << std::setw(20) << numCols << std::endl;
+  std::cout << std::setw(20) << std::left << "- # edges" << std::setw(20) << numEdges << std::endl;
+  std::cout << std::setw(20) << std::left << "- dataset" << std::setw(20) << "Load [OK]" << std::endl;
+  std::cout << std::setw(20) << std::left << "- load balance" << std::setw(20)
+            << (lb == BFS_LB_GLB ? "[GLOBAL]"
+                : lb == BFS_LB_SLB ? "[STRIDED-LOCAL]"
+                : lb == BFS_LB_LEARNED ? "[LEARNED]" : "[LOCAL]")
+            << std::endl;
+  std::cout << "----------------------------------------" << std::endl;
+  if ((uint32_t)start_vertex >= numCols) {
+    std::cerr << "ERROR: root " << start_vertex << " >= " << numCols << " vertices" << std::endl;
+    bfs_csc_host_free(&g);
+    return 1;
+  }
+
+  std::vector<uint32_t> indptr(g.indptr, g.indptr + (size_t)numCols + 1);
+  std::vector<uint32_t> inds(g.inds, g.inds + g.nnz);
+  bfs_csc_host_free(&g);
+  std::vector<int> h_dist(numCols, -1);
+  h_dist[(size_t)start_vertex] = 0;
+  std::vector<std::vector<int>> h_distancesGPU((size_t)num_runs, h_dist);
+  std::vector<uint8_t> h_updating_graph_mask(numCols, 0), h_graph_visited(numCols, 0);
+  h_graph_visited[(size_t)start_vertex] = 1;
+  std::vector<uint32_t> h_visit_offsets = {0, numRows};
+
+  bfs::GpuRunConfig &cfg = bfs::gpurun_config();
+  cfg.lb = lb;
+  cfg.block = block;
+  cfg.ipt = ipt;
+  cfg.loop = parser.get("loop") == "host" ? BFS_LOOP_HOST : BFS_LOOP_GRAPH;
+  cfg.weights = lb == BFS_LB_LEARNED ? parser.get("weights") : "";
+  bfs::Json obj = bfs::Json::object();
+  try {
+    bfs::GPURun(numRows, inds, indptr, h_updating_graph_mask, h_graph_visited, h_distancesGPU,
+                start_vertex, num_runs, obj, h_visit_offsets);
+  } catch (const std::exception &e) {
+    std::cerr << "ERROR: " << e.what() << std::endl;
+    return 1;
+  }
+
+  const int maxLevel = *std::max_element(h_distancesGPU[0].begin(), h_distancesGPU[0].end()) + 2;
+  bool all_equal = true;
+  for (int i = 0; i + 1 < num_runs; i++)
+    all_equal = all_equal && h_distancesGPU[(size_t)i] == h_distancesGPU.back();
+  const bool status = all_equal && cfg.validation_errors == 0;
+  std::cout << "- GPU : ";
+  for (int i = 0; i < maxLevel; i++)
+    std::cout << std::count(h_distancesGPU.back().begin(), h_distancesGPU.back().end(), i) << ", ";
+  std::cout << "\n- CHECK: " << cfg.validation_errors << " level violations on the device, runs "
+            << (all_equal ? "agree" : "DIFFER") << std::endl;
+  std::cout << "----------------------------------------" << std::endl;
+  std::cout << (status ? "[SUCCESS]" : "[FAILURE]") << "\tAll results on GPUs (" << num_runs
+            << " runs) cross checked\n";
+  std::cout << "----------------------------------------" << std::endl;
+
+  const double edges = (double)cfg.edges_count;
+  const double avg_ms = obj["avgExecutionTime"].as_double();
+  const double avg90 = obj["avgExecutionTime90f"].as_double();
+  const double avgf = obj["avgExecutionTimeFiltered"].as_double();
+  const double minf = obj["minExecutionTimeFiltered"].as_double();
+  obj["edgesCount"] = (unsigned long long)cfg.edges_count;
+  obj["valid"] = status;
+  obj["startVertex"] = start_vertex;
+  obj["numLevels"] = maxLevel - 1;
+  obj["avgMTEPS"] = edges / (1e6 * avg_ms * 1e-3);
+  obj["avgMTEPS90f"] = edges / (1e6 * avg90 * 1e-3);
+  {
+    std::ostringstream gs;
+    gs << std::fixed << std::setprecision(2) << edges / (1e9 * avg90 * 1e-3);
+    obj["avgGTEPS90f"] = gs.str();
+  }
+  obj["avgMTEPSFilter"] = edges / (1e6 * avgf * 1e-3);
+  obj["maxMTEPSFilter"] = edges / (1e6 * minf * 1e-3);
+  obj["edgesCoverage"] = numEdges ? 100.0 * edges / (double)numEdges : 0.0;
+  bfs::Json levels = bfs::Json::array();
+  for (int i = 0; i < maxLevel - 1; i++)
+    levels.push_back((long long)std::count(h_distancesGPU.back().begin(),
+                                           h_distancesGPU.back().end(), i));
+  obj["LevelsGPU"] = levels;
+  obj["variant"] = variant_key(lb < 0 ? bfs::default_lb() : lb);
+  obj["blockSize"] = block;
+  obj["validationErrors"] = (unsigned long long)cfg.validation_errors;
+
+  bfs::Json combined = bfs::Json::object();
+  {
+    std::ifstream in(output);
+    if (in.is_open()) {
+      std::stringstream ss;
+      ss << in.rdbuf();
+      try {
+        combined = bfs::Json::parse(ss.str());
+        if (!combined.is_object()) combined = bfs::Json::object();
+      } catch (const std::exception &e) {
+        std::cerr << "Error reading or parsing existing JSON data: " << e.what() << std::endl;
+        combined = bfs::Json::object();
+      }
+    }
+  }
+  const std::string key = dataset + "_" + std::to_string(num_runs) + "_" +
+                          variant_key(lb < 0 ? bfs::default_lb() : lb);
+  combined[key][std::to_string(parts)] = obj;
+  std::ofstream out(output);
+  if (!out.is_open()) {
+    std::cerr << "Error opening file for writing." << std::endl;
+    return 1;
+  }
+  out << combined.dump(4);
+  return status ? 0 : 2;
+}

@@ -146,6 +146,9 @@ bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,
  * number of violations (0 = valid). */
 bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,
                                const int32_t *parents_dev, uint64_t *bad);
+/* Same checks for a host level array (copied to the device first). */
+bfs_status bfs_validate_host(bfs_graph *g, uint32_t root, const int32_t *levels_host,
+                             uint64_t *bad);
 
 /* ---- batched multi-source BFS ------------------------------------------ */
 /* n_roots independent BFS runs on one graph, 64 roots per pass: each vertex

@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="level-loop driver (host: every kernel a plain launch, for ncu)")
     ap.add_argument("--skip-batched", action="store_true", help="omit the batched leg")
+    ap.add_argument("--skip-multigraph", action="store_true",
+                    help="omit the 256-graph single-launch leg")
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-arms", action="store_true", help="omit the per-arm table")
@@ -319,6 +321,47 @@ def run_gb300(a):
                    "workload": f"64 seeded roots on the same RMAT-{a.scale} graph, device "
                                "CUDA-event time of one bfs_run_batch pass vs 64 bfs_run_device"}
 
+    # many small graphs: 256 uneven R-MAT graphs (scales 10-16, EF16, seeds
+    # 100-355), one root each, one autotuned CUDA-graph launch vs one
+    # single-graph BFS after another
+    multigraph = None
+    if not a.skip_multigraph:
+        import tempfile
+        graphs, mroots = B.multi_batch_graphs(B.multi_batch_specs())
+        mb = B.MultiBatch(graphs)
+        mout = torch.empty(mb.total_cols, dtype=torch.int32, device="cuda")
+        cache = os.path.join(tempfile.gettempdir(), "bfs_gb300_multigraph_autotune.tsv")
+        best, tune_ms = mb.autotune(mroots, mout.data_ptr(), reps=3, cache_path=cache)
+        mb.run(mroots, mout.data_ptr(), *best)
+        mms = sorted(mb.run(mroots, mout.data_ptr(), *best)[1] for _ in range(5))
+        m_ms = mms[len(mms) // 2]
+        seq_plain, seq_graph = 0.0, 0.0
+        handles = [B.Graph.upload(g, validate=False) for g in graphs]
+        for h, r in zip(handles, mroots):
+            slv = torch.empty(h.n_cols, dtype=torch.int32, device="cuda")
+            h.run_device(int(r), slv.data_ptr(), opts=B.options("llb", 256, loop="host"))
+            seq_plain += h.run_device(int(r), slv.data_ptr(),
+                                      opts=B.options("llb", 256, loop="host")).device_ms
+            h.run_device(int(r), slv.data_ptr(), opts=B.options("llb", 256))
+            seq_graph += h.run_device(int(r), slv.data_ptr(),
+                                      opts=B.options("llb", 256)).device_ms
+            h.free()
+        mb.free()
+        del mout
+        multigraph = {
+            "graphs_per_s": round(len(graphs) / (m_ms * 1e-3), 1),
+            "launch_ms": round(m_ms, 4),
+            "autotuned": {"block": best[0], "items_per_thread": best[1],
+                          "times_ms": {f"{b}x{p}": round(t, 4)
+                                       for (b, p), t in zip(B.MULTI_CONFIGS, tune_ms)}},
+            "sequential_plain_launches_graphs_per_s": round(len(graphs) / (seq_plain * 1e-3), 1),
+            "sequential_graph_loop_graphs_per_s": round(len(graphs) / (seq_graph * 1e-3), 1),
+            "speedup_vs_sequential_plain_launches": round(seq_plain / m_ms, 2),
+            "speedup_vs_sequential_graph_loop": round(seq_graph / m_ms, 2),
+            "workload": "256 R-MAT graphs, scales drawn from 10-16, EF16, seeds 100-355, one "
+                        "root each; one persistent CUDA-graph launch vs 256 single-graph BFS "
+                        "(LLB/256, device time summed)"}
+
     # CPU baseline: the oracle on one root, one thread (rank 0 only)
     cpu = None
     if rank == 0 and not a.skip_cpu:
@@ -368,6 +411,7 @@ def run_gb300(a):
         "fixed_llb256": {"value": round(llb_gteps, 4), "unit": UNIT},
         "learned_vs_fixed_llb256": round(value / llb_gteps, 3) if a.lb == "learned" else None,
         "batched": batched,
+        "multigraph": multigraph,
         "arms_gteps": arms,
         "levels_first_root": lvl_rows,
     }

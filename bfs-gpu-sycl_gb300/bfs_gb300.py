@@ -137,6 +137,14 @@ def lib():
     _sig(L, "bfs_sched_attach", [VP, C.POINTER(C.c_float), C.c_float])
     _sig(L, "bfs_run_batch", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
                               C.POINTER(BatchStats)])
+    _sig(L, "bfs_multi_create", [C.c_uint32, C.POINTER(U32P), C.POINTER(U32P), U32P, U32P,
+                                 C.POINTER(C.c_uint64), C.POINTER(VP)])
+    _sig(L, "bfs_multi_free", [VP])
+    _sig(L, "bfs_multi_level_offset", [VP, C.c_uint32, C.POINTER(C.c_uint64)])
+    _sig(L, "bfs_multi_run", [VP, U32P, C.c_int32, C.c_int32, VP, C.POINTER(C.c_uint64),
+                              C.POINTER(C.c_double)])
+    _sig(L, "bfs_multi_autotune", [VP, U32P, VP, C.c_int32, C.c_char_p, I32P, I32P,
+                                   C.POINTER(C.c_float)])
     _lib = L
     return L
 
@@ -294,6 +302,84 @@ def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=
     o.record = int(record)
     o.ipt = int(ipt)
     return o
+
+
+MULTI_CONFIGS = [(b, p) for b in (128, 256, 512) for p in (1, 2, 4)]
+
+
+def multi_batch_specs(n=256, first_seed=100, scales=(10, 16), edge_factor=16):
+    """(scale, edge_factor, seed) of the uneven R-MAT batch: seeds first_seed ..
+    first_seed + n - 1, scales drawn uniformly from the closed range with a
+    fixed-seed numpy generator (identical on every machine)."""
+    rng = np.random.default_rng(20251203)
+    sc = rng.integers(scales[0], scales[1] + 1, size=n)
+    return [(int(sc[i]), edge_factor, first_seed + i) for i in range(n)]
+
+
+def multi_batch_graphs(specs):
+    """Host-generated graphs and one seeded root (degree > 0) per graph."""
+    graphs, roots = [], []
+    for scale, ef, seed in specs:
+        g = gen_rmat(scale, ef, seed=seed)
+        graphs.append(g)
+        roots.append(int(sample_roots(g, 1, seed)[0]))
+    return graphs, np.array(roots, np.uint32)
+
+
+class MultiBatch:
+    """Many small graphs packed on the device for single-launch BFS."""
+
+    def __init__(self, graphs):
+        self._keep = [(np.ascontiguousarray(g.indptr, np.uint32),
+                       np.ascontiguousarray(g.inds if g.nnz else np.zeros(1, np.uint32),
+                                            np.uint32)) for g in graphs]
+        n = len(graphs)
+        ips = (U32P * n)(*[k[0].ctypes.data_as(U32P) for k in self._keep])
+        ixs = (U32P * n)(*[k[1].ctypes.data_as(U32P) for k in self._keep])
+        rows = np.array([g.n_rows for g in graphs], np.uint32)
+        cols = np.array([g.n_cols for g in graphs], np.uint32)
+        nnz = np.array([g.nnz for g in graphs], np.uint64)
+        self.h = VP()
+        check(lib().bfs_multi_create(n, ips, ixs, rows.ctypes.data_as(U32P),
+                                     cols.ctypes.data_as(U32P),
+                                     nnz.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(self.h)))
+        self.n_graphs = n
+        self.n_cols = cols
+        self.total_cols = int(cols.astype(np.int64).sum())
+        self._keep = None
+
+    def offset(self, g):
+        off = C.c_uint64(0)
+        check(lib().bfs_multi_level_offset(self.h, g, C.byref(off)))
+        return off.value
+
+    def run(self, roots, levels_ptr, block=256, ipt=2):
+        rt = np.ascontiguousarray(roots, np.uint32)
+        ec = np.zeros(self.n_graphs, np.uint64)
+        ms = C.c_double(0)
+        check(lib().bfs_multi_run(self.h, rt.ctypes.data_as(U32P), block, ipt, VP(levels_ptr),
+                                  ec.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(ms)))
+        return ec, ms.value
+
+    def autotune(self, roots, levels_ptr, reps=3, cache_path=None):
+        rt = np.ascontiguousarray(roots, np.uint32)
+        b, p = C.c_int32(0), C.c_int32(0)
+        t = (C.c_float * len(MULTI_CONFIGS))()
+        check(lib().bfs_multi_autotune(self.h, rt.ctypes.data_as(U32P), VP(levels_ptr), reps,
+                                       cache_path.encode() if cache_path else None, C.byref(b),
+                                       C.byref(p), t))
+        return (b.value, p.value), list(t)
+
+    def free(self):
+        if self.h:
+            lib().bfs_multi_free(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Graph:

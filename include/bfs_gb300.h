@@ -167,6 +167,34 @@ bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
                          int32_t *levels_dev, uint64_t *edges_count_out,
                          bfs_batch_stats *stats);
 
+/* ---- many small graphs in one launch ----------------------------------- */
+/* A batch of independent graphs (up to 2^18 vertices each) packed into one
+ * CSC in HBM; bfs_multi_run runs one BFS per graph from roots[g] in a single
+ * persistent kernel captured in a CUDA graph: each block claims whole graphs,
+ * largest first, and runs their level loop on its own with the visited bitmap
+ * in shared memory.  The reference needs one process run per graph and root
+ * (src/host.cpp:57-276). */
+typedef struct bfs_multi bfs_multi;
+bfs_status bfs_multi_create(uint32_t n_graphs, const uint32_t *const *indptrs,
+                            const uint32_t *const *inds, const uint32_t *n_rows,
+                            const uint32_t *n_cols, const uint64_t *nnz, bfs_multi **out);
+bfs_status bfs_multi_free(bfs_multi *m);
+/* Offset of graph g's level array inside the packed output (sum of the
+ * n_cols of the graphs before it). */
+bfs_status bfs_multi_level_offset(const bfs_multi *m, uint32_t graph, uint64_t *offset);
+/* levels_dev: sum of n_cols int32 (device).  block 128/256/512, ipt 1/2/4
+ * (warp rounds in flight per lane).  edges_count_out: n_graphs (host,
+ * optional); device_ms: CUDA-event time of the launch (optional). */
+bfs_status bfs_multi_run(bfs_multi *m, const uint32_t *roots, int32_t block, int32_t ipt,
+                         int32_t *levels_dev, uint64_t *edges_count_out, double *device_ms);
+/* Times every (block, ipt) combination on this batch (best of reps) and
+ * returns the fastest.  With cache_path, a previous result for the same GPU
+ * and batch shape is reused and a new one is appended.  times_ms (optional)
+ * receives the 9 timings, block-major (-1 when taken from the cache). */
+bfs_status bfs_multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
+                              int32_t reps, const char *cache_path, int32_t *best_block,
+                              int32_t *best_ipt, float *times_ms);
+
 /* ---- BFS without device allocation ------------------------------------ */
 /* No counterpart in the reference (its GPURun allocates per run).  For
  * callers that cannot allocate device memory -- code inside an allocator or

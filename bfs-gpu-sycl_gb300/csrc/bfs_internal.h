@@ -103,6 +103,7 @@ struct BfsDevState {
   uint32_t reached_prev; // `reached` before the current level generation
   uint32_t max_level;    // deepest level that received a vertex
   uint32_t done_blocks;  // level-generation blocks finished this level
+  uint32_t lg_cursor;    // next bitmap word to claim in level generation
   uint32_t error;        // non-zero: internal error flag
   uint32_t launches;     // kernels launched in the device loop
   int32_t arm;           // explore arm chosen for the current level

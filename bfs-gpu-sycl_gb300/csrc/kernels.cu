@@ -118,6 +118,7 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
   st->max_level = 0;
   st->next_packed = 0;
   st->done_blocks = 0;
+  st->lg_cursor = 0;
   st->error = 0;
   st->launches = 2;
   st->arm = st->fixed_arm >= 0 ? st->fixed_arm : 0;
@@ -136,8 +137,19 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
 // exclusive scan of the tile's degrees (shared memory) splits the tile's
 // edges evenly over the block's warps (block-local balancing, :437-445).
 // U warp rounds (U edges per lane) are resolved before their loads issue.
+// Minimum resident blocks requested from the compiler (register budget).
+// Measured on RMAT-25: 2048 resident threads per SM (32 registers) for 4
+// rounds per lane make GLB and SLB faster despite a few spilled bytes; LLB's
+// large-tile level is faster at 1536 threads (40 registers).  8 rounds per
+// lane get 1024 threads (64 registers).
+template <int B, int U, bool CONSTRAINED>
+struct MinBlocks {
+  static constexpr int value = (U <= 4 ? (CONSTRAINED ? 2048 : 1536) : 1024) / B;
+};
+
 template <int B, bool STRIDED, int U>
-__global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restrict__ st) {
+__global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
+    explore_local_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
   __shared__ uint32_t s_off[B + 1];
   __shared__ uint32_t s_beg[B];
@@ -234,9 +246,11 @@ __global__ void __launch_bounds__(B) explore_local_kernel(BfsDevState *__restric
 // next 32 entry starts and first-edge offsets coalesced, and every lane takes
 // its owner's offsets from those registers with shuffles.
 template <int B, int U>
-__global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restrict__ st) {
+__global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
+    explore_global_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
-  constexpr uint32_t CHUNK = 32u * U * kGlbGroups;  // edges per warp chunk
+  constexpr uint32_t kRound = 32u * U;
+  constexpr uint32_t kMinChunk = kRound * kGlbGroups;
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t EF = st->EF;
@@ -249,25 +263,32 @@ __global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restri
   int32_t *parent = st->parent;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
-  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
   const uint32_t total_warps = gridDim.x * NW;
+  // about four chunks per warp (each chunk costs one owner search), whole
+  // groups of U rounds, at least kMinChunk edges
+  uint64_t ch = ((uint64_t)EF + 4ull * total_warps - 1) / (4ull * total_warps);
+  ch = (ch + kRound - 1) / kRound * kRound;
+  const uint32_t CHUNK = (uint32_t)(ch > kMinChunk ? ch : kMinChunk);
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
 
   for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
-    const uint32_t w0 = c * CHUNK;
+    const uint32_t w0 = c * CHUNK;  // < EF, no overflow
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
     uint32_t cur_start = qp[cur], cur_beg = qb[cur];
     uint32_t cur_vid = parent ? qv[cur] : 0u;
-    for (uint32_t base = w0; base < w1; base += 32u * U) {
+    // starts / first edges / ids of the 32 entries after cur; reloaded only
+    // when the owner of the last lane moves past cur
+    uint32_t j = cur + 1u + lane;
+    uint32_t bnd = (j <= F) ? qp[j] : kFull;  // qp[F] = EF
+    uint32_t bg = (j < F) ? qb[j] : 0u;
+    uint32_t vd = (parent && j < F) ? qv[j] : 0u;
+    for (uint32_t base = w0; base < w1; base += kRound) {
       uint32_t addr[U], from[U];
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
         const uint32_t e = rb + lane;
-        const uint32_t j = cur + 1u + lane;
-        const uint32_t bnd = (j <= F) ? qp[j] : kFull;  // qp[F] = EF
-        const uint32_t bg = (j < F) ? qb[j] : 0u;
-        const uint32_t vd = (parent && j < F) ? qv[j] : 0u;
         const uint32_t p = bnd - rb;
         const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
         const uint32_t k = __popc(starts & ((2u << lane) - 1u));
@@ -288,6 +309,10 @@ __global__ void __launch_bounds__(B) explore_global_kernel(BfsDevState *__restri
           cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
           cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
           cur_vid = __shfl_sync(kFull, vd, k31 - 1u);
+          j = cur + 1u + lane;
+          bnd = (j <= F) ? qp[j] : kFull;
+          bg = (j < F) ? qb[j] : 0u;
+          vd = (parent && j < F) ? qv[j] : 0u;
         }
       }
       uint32_t nb[U];
@@ -318,6 +343,7 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
   st->lvl = lvl;
   st->next_packed = 0;
   st->done_blocks = 0;
+  st->lg_cursor = 0;
   st->launches += 2;
   if (lvl < st->rec_cap) {
     st->rec_frontier[lvl] = f_new;
@@ -331,14 +357,51 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
 }
 
+// Level generation.  Blocks claim spans of NW * kLgGroups * 32 bitmap words
+// from a counter (dense regions of the bitmap are uneven), and a warp owns
+// kLgGroups groups of 32 words of the span.  In each group the new vertices (vis & ~prev) are processed
+// flattened: lane l of round r takes the (32 r + l)-th new vertex of the
+// group, so 32 indptr loads are in flight per round whatever the bit layout.
+// Pass 1 writes levels and counts kept entries and their degrees; one atomic
+// per block and step reserves queue slots and edge offsets; pass 2 re-reads
+// the (now cached) indptr pairs and writes the entries.
+constexpr int kLgGroups = 2;
+
+// Word (0..31) holding the t-th new vertex of a group, given each lane's
+// inclusive prefix of per-word new counts (binary search over the lanes).
+__device__ __forceinline__ uint32_t lg_word_of(uint32_t incl, uint32_t t) {
+  uint32_t lo = 0, hi = 31;  // the answer is <= 31 because t < incl of lane 31
+#pragma unroll
+  for (int s = 0; s < 5; s++) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t im = __shfl_sync(kFull, incl, mid);
+    if (im <= t) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Position (0..31) of the set bit of rank n (0-based) in x, for n < popc(x):
+// the smallest p with popc(x & bits[0..p]) > n.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t x, uint32_t n) {
+  uint32_t lo = 0, hi = 31;
+#pragma unroll
+  for (int s = 0; s < 5; s++) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((uint32_t)__popc(x & ((2u << mid) - 1u)) > n) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
 template <int B>
 __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ st,
                                                      unsigned long long cond,
                                                      int use_cond) {
   constexpr int NW = B / 32;
+  constexpr uint32_t kSpan = 32u * kLgGroups;  // words per warp and step
   __shared__ unsigned long long s_wtot[NW];
   __shared__ unsigned long long s_base;
   __shared__ uint32_t s_reached[NW];
+  __shared__ uint32_t s_sb;
   __shared__ int s_last;
 
   const uint32_t words = st->words;
@@ -356,67 +419,89 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t reached = 0;
 
-  for (uint32_t sb = blockIdx.x * (NW * 32u); sb < words; sb += gridDim.x * (NW * 32u)) {
-    const uint32_t gw = sb + warp * 32u;  // first of this warp's 32 words
-    const uint32_t w = gw + lane;
-    uint32_t newb = 0;
-    if (gw < words) {
-      const uint32_t vw = V[w], pw = P[w];
-      newb = vw & ~pw;
-      if (newb) P[w] = vw;
-    }
-    reached += __popc(newb);
-    const uint32_t nz = __ballot_sync(kFull, newb != 0u);
-    // pass 1: levels, kept entries and their degrees per word
-    unsigned long long mine = 0;  // (count << 32 | degree sum) of word `lane`
-    for (uint32_t m = nz; m; m &= m - 1u) {
-      const uint32_t src = __ffs(m) - 1u;
-      const uint32_t wb = __shfl_sync(kFull, newb, src);
-      const uint32_t v = (gw + src) * 32u + lane;
-      uint32_t deg = 0;
-      if ((wb >> lane) & 1u) {
-        level[v] = lvl_next;
-        if (v < n_rows) deg = indptr[v + 1] - indptr[v];
+  for (;;) {
+    if (threadIdx.x == 0) s_sb = atomicAdd(&st->lg_cursor, NW * kSpan);
+    __syncthreads();
+    const uint32_t sb = s_sb;
+    if (sb >= words) break;
+    const uint32_t gw0 = sb + warp * kSpan;  // first word of this warp's span
+    uint32_t newb[kLgGroups], incl[kLgGroups], tot[kLgGroups];
+#pragma unroll
+    for (int g = 0; g < kLgGroups; g++) {
+      const uint32_t w = gw0 + 32u * g + lane;
+      uint32_t nb = 0;
+      if (gw0 + 32u * g < words) {  // words is a multiple of 32
+        const uint32_t vw = V[w], pw = P[w];
+        nb = vw & ~pw;
+        if (nb) P[w] = vw;
       }
-      const uint32_t km = __ballot_sync(kFull, deg > 0u);
-      const uint32_t ds = __reduce_add_sync(kFull, deg);
-      if (lane == src) mine = ((unsigned long long)__popc(km) << 32) | ds;
+      newb[g] = nb;
+      reached += __popc(nb);
+      incl[g] = warp_incl_scan(__popc(nb), lane);
+      tot[g] = __shfl_sync(kFull, incl[g], 31);
     }
-    // block-wide offsets: warp scan, then one atomic per block
-    const unsigned long long incl = warp_incl_scan64(mine, lane);
-    if (lane == 31) s_wtot[warp] = incl;
+    // pass 1: levels; kept-entry count and degree sum of the warp
+    uint32_t w_cnt = 0, w_deg = 0;
+#pragma unroll
+    for (int g = 0; g < kLgGroups; g++) {
+      for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u) {
+        const uint32_t t = t0 + lane;
+        const uint32_t wd = lg_word_of(incl[g], t < tot[g] ? t : tot[g] - 1u);
+        const uint32_t bits = __shfl_sync(kFull, newb[g], wd);
+        const uint32_t ex = __shfl_sync(kFull, incl[g], wd) - __popc(bits);
+        uint32_t deg = 0;
+        if (t < tot[g]) {
+          const uint32_t v = (gw0 + 32u * g + wd) * 32u + nth_set_bit(bits, t - ex);
+          level[v] = lvl_next;
+          if (v < n_rows) deg = indptr[v + 1] - indptr[v];
+        }
+        w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
+        w_deg += __reduce_add_sync(kFull, deg);
+      }
+    }
+    // block-wide offsets: one atomic per block and step
+    if (lane == 0) s_wtot[warp] = ((unsigned long long)w_cnt << 32) | w_deg;
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned long long run = 0;
       for (int i = 0; i < NW; i++) {
-        const unsigned long long t = s_wtot[i];
+        const unsigned long long x = s_wtot[i];
         s_wtot[i] = run;
-        run += t;
+        run += x;
       }
       s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
     }
     __syncthreads();
-    if (nz) {
-      const unsigned long long my_base = s_base + s_wtot[warp] + (incl - mine);
-      // pass 2: write the kept entries
-      for (uint32_t m = nz; m; m &= m - 1u) {
-        const uint32_t src = __ffs(m) - 1u;
-        const uint32_t wb = __shfl_sync(kFull, newb, src);
-        const unsigned long long wbase = __shfl_sync(kFull, my_base, src);
-        const uint32_t v = (gw + src) * 32u + lane;
-        uint32_t b = 0, e = 0;
-        if (((wb >> lane) & 1u) && v < n_rows) {
-          b = indptr[v];
-          e = indptr[v + 1];
-        }
-        const uint32_t deg = e - b;
-        const uint32_t km = __ballot_sync(kFull, deg > 0u);
-        const uint32_t dx = warp_incl_scan(deg, lane) - deg;
-        if (deg) {
-          const uint32_t slot = (uint32_t)(wbase >> 32) + __popc(km & lt_mask);
-          qb[slot] = b;
-          qp[slot] = (uint32_t)wbase + dx;
-          qv[slot] = v;
+    if (w_cnt) {
+      unsigned long long wb = s_base + s_wtot[warp];
+      uint32_t slot = (uint32_t)(wb >> 32), pref = (uint32_t)wb;
+      // pass 2: write the kept entries in the same order
+#pragma unroll
+      for (int g = 0; g < kLgGroups; g++) {
+        for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u) {
+          const uint32_t t = t0 + lane;
+          const uint32_t wd = lg_word_of(incl[g], t < tot[g] ? t : tot[g] - 1u);
+          const uint32_t bits = __shfl_sync(kFull, newb[g], wd);
+          const uint32_t ex = __shfl_sync(kFull, incl[g], wd) - __popc(bits);
+          uint32_t v = 0, b = 0, e = 0;
+          if (t < tot[g]) {
+            v = (gw0 + 32u * g + wd) * 32u + nth_set_bit(bits, t - ex);
+            if (v < n_rows) {
+              b = indptr[v];
+              e = indptr[v + 1];
+            }
+          }
+          const uint32_t deg = e - b;
+          const uint32_t km = __ballot_sync(kFull, deg > 0u);
+          const uint32_t dincl = warp_incl_scan(deg, lane);
+          if (deg) {
+            const uint32_t sl = slot + __popc(km & lt_mask);
+            qb[sl] = b;
+            qp[sl] = pref + dincl - deg;
+            qv[sl] = v;
+          }
+          slot += __popc(km);
+          pref += __shfl_sync(kFull, dincl, 31);
         }
       }
     }

@@ -9,8 +9,9 @@ namespace bfsgb {
 
 constexpr int kLevelgenBlock = 256;
 // Explore kernels keep U warp rounds (U edges per lane) in flight; U is the
-// "items per thread" tunable (4 or 8).  A GLB warp chunk is kGlbGroups groups
-// of U rounds.
+// "items per thread" tunable (4 or 8).  A GLB warp chunk is at least
+// kGlbGroups groups of U rounds (more when the level is large: about four
+// chunks per warp of the grid).
 constexpr int kGlbGroups = 4;
 inline uint32_t glb_chunk_edges(int ipt) { return 32u * (uint32_t)ipt * kGlbGroups; }
 

@@ -121,8 +121,10 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
   }
 }
 
-__global__ void __launch_bounds__(kMsBlock) ms_explore_kernel(MsState *__restrict__ st) {
+__global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
+    ms_explore_kernel(MsState *__restrict__ st) {
   constexpr int NW = kMsBlock / 32;
+  constexpr uint32_t kRound = 32u * kMsU;
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t EF = st->EF;
@@ -135,26 +137,30 @@ __global__ void __launch_bounds__(kMsBlock) ms_explore_kernel(MsState *__restric
   unsigned long long *next = st->next;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
-  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + kMsChunk - 1) / kMsChunk);
   const uint32_t total_warps = gridDim.x * NW;
+  // about four chunks per warp, whole groups of kMsU rounds
+  uint64_t ch = ((uint64_t)EF + 4ull * total_warps - 1) / (4ull * total_warps);
+  ch = (ch + kRound - 1) / kRound * kRound;
+  const uint32_t CHUNK = (uint32_t)(ch > kMsChunk ? ch : kMsChunk);
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
 
   for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
-    const uint32_t w0 = c * kMsChunk;
-    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + kMsChunk);
+    const uint32_t w0 = c * CHUNK;
+    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
     uint32_t cur_start = qp[cur], cur_beg = qb[cur];
     unsigned long long cur_mask = qm[cur];
-    for (uint32_t base = w0; base < w1; base += 32u * kMsU) {
+    uint32_t j = cur + 1u + lane;
+    uint32_t bnd = (j <= F) ? qp[j] : kFull;
+    uint32_t bg = (j < F) ? qb[j] : 0u;
+    unsigned long long mk = (j < F) ? qm[j] : 0ull;
+    for (uint32_t base = w0; base < w1; base += kRound) {
       uint32_t addr[kMsU];
       unsigned long long msk[kMsU];
 #pragma unroll
       for (int u = 0; u < kMsU; u++) {
         const uint32_t rb = base + 32u * u;
         const uint32_t e = rb + lane;
-        const uint32_t j = cur + 1u + lane;
-        const uint32_t bnd = (j <= F) ? qp[j] : kFull;
-        const uint32_t bg = (j < F) ? qb[j] : 0u;
-        const unsigned long long mk = (j < F) ? qm[j] : 0ull;
         const uint32_t p = bnd - rb;
         const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
         const uint32_t k = __popc(starts & ((2u << lane) - 1u));
@@ -174,6 +180,10 @@ __global__ void __launch_bounds__(kMsBlock) ms_explore_kernel(MsState *__restric
           cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
           cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
           cur_mask = __shfl_sync(kFull, mk, k31 - 1u);
+          j = cur + 1u + lane;
+          bnd = (j <= F) ? qp[j] : kFull;
+          bg = (j < F) ? qb[j] : 0u;
+          mk = (j < F) ? qm[j] : 0ull;
         }
       }
       uint32_t nb[kMsU];

@@ -304,33 +304,56 @@ def run_gb300(a):
                     ed += st.edges_count
                 arms[f"{lb}{blk}"] = round(ed / (ms * 1e-3) / 1e9, 3)
 
-    # batched: one 64-root multi-source pass vs 64 sequential runs
-    batched = None
+    # batched: multi-source passes of 64 roots vs 64 sequential runs.
+    # (1) the batched configuration: RMAT-22/EF16 seed 6, 1024 seeded roots in
+    #     16 passes; (2) one 64-root pass on this RMAT-25 graph.
+    batched = batched25 = None
     if not a.skip_batched:
-        broots = roots[:64] if len(roots) >= 64 else B.sample_roots(host, 64, a.seed + 7)
-        if len(broots) < 64:
-            broots = B.sample_roots(host, 64, a.seed + 7)
+        def seq_ms(graph, rs, o):
+            graph.run_device(int(rs[0]), seq_lv.data_ptr(), opts=o)
+            return sum(graph.run_device(int(r), seq_lv.data_ptr(), opts=o).device_ms
+                       for r in rs)
+
+        g22 = B.Graph.gen_rmat_device(22, 16, seed=6)
+        if weights is not None:
+            g22.sched_attach(weights)
+        r22 = B.sample_roots(g22.download(), 1024, 6)
+        out = torch.empty((64, g22.n_cols), dtype=torch.int32, device="cuda")
+        g22.run_batch(r22[:64], out.data_ptr(), want_edges=False)
+        b_ms = 0.0
+        for b in range(16):
+            _, bst = g22.run_batch(r22[64 * b:64 * (b + 1)], out.data_ptr(), want_edges=False)
+            b_ms += bst.device_ms
+        seq_lv = torch.empty(g22.n_cols, dtype=torch.int32, device="cuda")
+        s_llb = seq_ms(g22, r22[:64], B.options("llb", 256))
+        s_lrn = seq_ms(g22, r22[:64], B.options(a.lb, a.block))
+        batched = {"roots_per_s": round(1024 / (b_ms * 1e-3), 1),
+                   "ms_per_64_roots": round(b_ms / 16, 3),
+                   "sequential_llb256_roots_per_s": round(64 / (s_llb * 1e-3), 1),
+                   "sequential_learned_roots_per_s": round(64 / (s_lrn * 1e-3), 1),
+                   "speedup_vs_sequential_llb256": round(s_llb / (b_ms / 16), 2),
+                   "speedup_vs_sequential_learned": round(s_lrn / (b_ms / 16), 2),
+                   "workload": "RMAT-22/EF16 seed 6, 1024 seeded roots in 16 bfs_run_batch "
+                               "passes of 64 vs 64 sequential bfs_run_device runs (device "
+                               "CUDA-event time)"}
+        del out, seq_lv
+        g22.free()
+        broots = B.sample_roots(host, 64, a.seed + 7)
         out = torch.empty((64, n), dtype=torch.int32, device="cuda")
         dg.run_batch(broots, out.data_ptr(), want_edges=False)
-        bms = []
-        for _ in range(3):
-            _, bst = dg.run_batch(broots, out.data_ptr(), want_edges=False)
-            bms.append(bst.device_ms)
-        b_ms = min(bms)
-        seq = {}
-        for name, o in (("llb256", B.options("llb", 256)), ("learned", opts)):
-            seq[name] = sum(dg.run_device(int(r), lv.data_ptr(), opts=o).device_ms
-                            for r in broots)
+        bms = [dg.run_batch(broots, out.data_ptr(), want_edges=False)[1].device_ms
+               for _ in range(3)]
+        b25 = min(bms)
         del out
-        batched = {"roots_per_s": round(64 / (b_ms * 1e-3), 1),
-                   "batch64_ms": round(b_ms, 3),
-                   "sequential_llb256_roots_per_s": round(64 / (seq["llb256"] * 1e-3), 1),
-                   "sequential_learned_roots_per_s": round(64 / (seq["learned"] * 1e-3), 1),
-                   "speedup_vs_sequential_llb256": round(seq["llb256"] / b_ms, 2),
-                   "speedup_vs_sequential_learned": round(seq["learned"] / b_ms, 2),
-                   "levels": bst.max_levels,
-                   "workload": f"64 seeded roots on the same RMAT-{a.scale} graph, device "
-                               "CUDA-event time of one bfs_run_batch pass vs 64 bfs_run_device"}
+        seq_lv = torch.empty(n, dtype=torch.int32, device="cuda")
+        s_llb = seq_ms(dg, broots, B.options("llb", 256))
+        s_lrn = seq_ms(dg, broots, opts)
+        del seq_lv
+        batched25 = {"roots_per_s": round(64 / (b25 * 1e-3), 1), "batch64_ms": round(b25, 3),
+                     "sequential_llb256_roots_per_s": round(64 / (s_llb * 1e-3), 1),
+                     "sequential_learned_roots_per_s": round(64 / (s_lrn * 1e-3), 1),
+                     "speedup_vs_sequential_llb256": round(s_llb / b25, 2),
+                     "speedup_vs_sequential_learned": round(s_lrn / b25, 2)}
 
     # many small graphs: 256 uneven R-MAT graphs (scales 10-16, EF16, seeds
     # 100-355), one root each, one autotuned CUDA-graph launch vs one
@@ -427,6 +450,7 @@ def run_gb300(a):
         "fixed_llb256": {"value": round(llb_gteps, 4), "unit": UNIT},
         "learned_vs_fixed_llb256": round(value / llb_gteps, 3) if a.lb == "learned" else None,
         "batched": batched,
+        "batched_rmat25": batched25,
         "multigraph": multigraph,
         "arms_gteps": arms,
         "levels_first_root": lvl_rows,

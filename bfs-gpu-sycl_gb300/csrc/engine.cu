@@ -135,8 +135,8 @@ static bfs_status setup_workspace(bfs_graph *g) {
   for (int u = 0; u < 2; u++) {
     for (int arm = 0; arm < kNumArms; arm++) {
       int occ = 0;
-      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, explore_kernel_fn(arm, u ? 8 : 4),
-                                                       arm_block(arm), 0));
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &occ, explore_kernel_fn(arm, u ? 8 : 4, false), arm_block(arm), 0));
       g->occ[u][arm] = std::max(occ, 1);
     }
   }
@@ -282,8 +282,8 @@ cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32
   void *args[] = {&st};
   const int grid = persistent ? persistent_blocks(g, arm, sm_factor, ipt)
                               : host_blocks(g, arm, sm_factor, ipt, F, EF);
-  return cudaLaunchKernel(explore_kernel_fn(arm, ipt), dim3(grid), dim3(arm_block(arm)), args, 0,
-                          g->stream);
+  return cudaLaunchKernel(explore_kernel_fn(arm, ipt, g->run_parents), dim3(grid),
+                          dim3(arm_block(arm)), args, 0, g->stream);
 }
 
 static void set_window(const bfs_graph *g, cudaGraphNode_t node) {
@@ -350,7 +350,7 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
 
   void *ex_args[] = {&st};
   if (arm >= 0) {
-    CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt),
+    CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt, g->run_parents),
                   persistent_blocks(g, arm, sm_factor, ipt), arm_block(arm), ex_args));
     set_window(g, n_explore);
   } else {
@@ -372,7 +372,8 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
     CK(cudaGraphAddNode(&n_explore, body, &n_sched, nullptr, 1, &sp));
     for (int a = 0; a < kNumArms; a++) {
       cudaGraphNode_t n_arm;
-      CK(add_kernel(sp.conditional.phGraph_out[a], &n_arm, nullptr, 0, explore_kernel_fn(a, ipt),
+      CK(add_kernel(sp.conditional.phGraph_out[a], &n_arm, nullptr, 0,
+                    explore_kernel_fn(a, ipt, g->run_parents),
                     persistent_blocks(g, a, sm_factor, ipt), arm_block(a), ex_args));
       set_window(g, n_arm);
     }
@@ -387,7 +388,8 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
 
 static bfs_status get_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt,
                                  GraphEntry **out) {
-  const int key = (arm + 1) * 4096 + (ipt == 8 ? 2048 : 0) + (g->use_l2_pin ? 1024 : 0) + sm_factor;
+  const int key = (arm + 1) * 8192 + (g->run_parents ? 4096 : 0) + (ipt == 8 ? 2048 : 0) +
+                  (g->use_l2_pin ? 1024 : 0) + sm_factor;
   auto it = g->graphs.find(key);
   if (it != g->graphs.end()) {
     *out = &it->second;
@@ -492,6 +494,7 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
   if (o.ipt != 4 && o.ipt != 8) return fail(BFS_ERR_INVALID_ARG, "ipt must be 4 or 8");
   CK(cudaSetDevice(g->device));
   g->use_l2_pin = o.l2_pin != 0;
+  g->run_parents = parents_dev != nullptr;
   if (o.loop == BFS_LOOP_HOST) {
     cudaStreamAttrValue v;
     std::memset(&v, 0, sizeof(v));

@@ -67,6 +67,7 @@ struct bfs_graph {
   int lg_grid = 0;
   bool l2_pinned = false;
   bool use_l2_pin = true;
+  bool run_parents = false;  // current run records parents
   cudaAccessPolicyWindow l2_window{};
   std::map<int, bfsgb::GraphEntry> graphs;
   int32_t host_arms[BFS_MAX_RECORDED_LEVELS] = {};

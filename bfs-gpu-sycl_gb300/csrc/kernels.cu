@@ -147,7 +147,7 @@ struct MinBlocks {
   static constexpr int value = (U <= 4 ? (CONSTRAINED ? 2048 : 1536) : 1024) / B;
 };
 
-template <int B, bool STRIDED, int U>
+template <int B, bool STRIDED, int U, bool PAR>
 __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     explore_local_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
   const uint32_t *__restrict__ qv = st->qv[cur_q];
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
-  int32_t *parent = st->parent;
+  int32_t *parent = PAR ? st->parent : nullptr;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t num_tiles = (F + B - 1) / B;
   const uint64_t pol = evict_first_policy();
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     if (slot < F) {
       beg = qb[slot];
       deg = qp[slot + 1] - qp[slot];
-      if (parent) vid = qv[slot];
+      if (PAR) vid = qv[slot];
     }
     const uint32_t incl = warp_incl_scan(deg, lane);
     if (lane == 31) s_wsum[warp] = incl;
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     const uint32_t total = s_wsum[NW - 1];
     s_off[threadIdx.x] = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
     s_beg[threadIdx.x] = beg;
-    s_vid[threadIdx.x] = vid;
+    if (PAR) s_vid[threadIdx.x] = vid;
     if (threadIdx.x == 0) s_off[B] = total;
     __syncthreads();
 
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
           from[u] = 0;
           if (e < w1) {
             addr[u] = s_beg[o] + (e - s_off[o]);
-            from[u] = s_vid[o];
+            if (PAR) from[u] = s_vid[o];
           }
           cur = __shfl_sync(kFull, o, 31);
           if (cur >= (uint32_t)B) cur = B - 1;  // only reached past w1
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
         for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
 #pragma unroll
         for (int u = 0; u < U; u++)
-          if (addr[u] != kFull) visit(vis, nb[u], parent, from[u]);
+          if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
       }
     }
     __syncthreads();
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
 // (one probe per lane and round), then walks forward: each round loads the
 // next 32 entry starts and first-edge offsets coalesced, and every lane takes
 // its owner's offsets from those registers with shuffles.
-template <int B, int U>
+template <int B, int U, bool PAR>
 __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
     explore_global_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
   const uint32_t *__restrict__ qv = st->qv[cur_q];
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
-  int32_t *parent = st->parent;
+  int32_t *parent = PAR ? st->parent : nullptr;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
   const uint32_t total_warps = gridDim.x * NW;
@@ -276,13 +276,13 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
     uint32_t cur_start = qp[cur], cur_beg = qb[cur];
-    uint32_t cur_vid = parent ? qv[cur] : 0u;
+    uint32_t cur_vid = PAR ? qv[cur] : 0u;
     // starts / first edges / ids of the 32 entries after cur; reloaded only
     // when the owner of the last lane moves past cur
     uint32_t j = cur + 1u + lane;
     uint32_t bnd = (j <= F) ? qp[j] : kFull;  // qp[F] = EF
     uint32_t bg = (j < F) ? qb[j] : 0u;
-    uint32_t vd = (parent && j < F) ? qv[j] : 0u;
+    uint32_t vd = (PAR && j < F) ? qv[j] : 0u;
     for (uint32_t base = w0; base < w1; base += kRound) {
       uint32_t addr[U], from[U];
 #pragma unroll
@@ -295,12 +295,12 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
         const uint32_t srcl = k ? k - 1u : 0u;
         const uint32_t s_start = __shfl_sync(kFull, bnd, srcl);
         const uint32_t s_beg = __shfl_sync(kFull, bg, srcl);
-        const uint32_t s_vid = __shfl_sync(kFull, vd, srcl);
+        const uint32_t s_vid = PAR ? __shfl_sync(kFull, vd, srcl) : 0u;
         addr[u] = kFull;
         from[u] = 0;
         if (e < w1) {
           addr[u] = (k ? s_beg : cur_beg) + (e - (k ? s_start : cur_start));
-          from[u] = k ? s_vid : cur_vid;
+          if (PAR) from[u] = k ? s_vid : cur_vid;
         }
         // carry the owner of lane 31 into the next round
         const uint32_t k31 = __shfl_sync(kFull, k, 31);
@@ -308,11 +308,11 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
           cur += k31;
           cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
           cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
-          cur_vid = __shfl_sync(kFull, vd, k31 - 1u);
+          if (PAR) cur_vid = __shfl_sync(kFull, vd, k31 - 1u);
           j = cur + 1u + lane;
           bnd = (j <= F) ? qp[j] : kFull;
           bg = (j < F) ? qb[j] : 0u;
-          vd = (parent && j < F) ? qv[j] : 0u;
+          vd = (PAR && j < F) ? qv[j] : 0u;
         }
       }
       uint32_t nb[U];
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
       for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
 #pragma unroll
       for (int u = 0; u < U; u++)
-        if (addr[u] != kFull) visit(vis, nb[u], parent, from[u]);
+        if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
     }
   }
 }
@@ -392,6 +392,19 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t x, uint32_t n) {
   return lo;
 }
 
+constexpr int kLgUnroll = 4;
+
+// Vertex of the t-th new bit of a group of 32 words starting at word w0, or
+// kFull when t is past the group's total (all lanes take part: shuffles).
+__device__ __forceinline__ uint32_t lg_vertex(uint32_t newb, uint32_t incl, uint32_t tot,
+                                              uint32_t t, uint32_t w0) {
+  const uint32_t wd = lg_word_of(incl, t < tot ? t : (tot ? tot - 1u : 0u));
+  const uint32_t bits = __shfl_sync(kFull, newb, wd);
+  const uint32_t ex = __shfl_sync(kFull, incl, wd) - __popc(bits);
+  if (t >= tot) return kFull;
+  return (w0 + wd) * 32u + nth_set_bit(bits, t - ex);
+}
+
 template <int B>
 __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ st,
                                                      unsigned long long cond,
@@ -440,23 +453,36 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
       incl[g] = warp_incl_scan(__popc(nb), lane);
       tot[g] = __shfl_sync(kFull, incl[g], 31);
     }
-    // pass 1: levels; kept-entry count and degree sum of the warp
+    // pass 1: levels; kept-entry count and degree sum of the warp.  kLgUnroll
+    // rounds are resolved first so their indptr loads are in flight together.
     uint32_t w_cnt = 0, w_deg = 0;
 #pragma unroll
     for (int g = 0; g < kLgGroups; g++) {
-      for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u) {
-        const uint32_t t = t0 + lane;
-        const uint32_t wd = lg_word_of(incl[g], t < tot[g] ? t : tot[g] - 1u);
-        const uint32_t bits = __shfl_sync(kFull, newb[g], wd);
-        const uint32_t ex = __shfl_sync(kFull, incl[g], wd) - __popc(bits);
-        uint32_t deg = 0;
-        if (t < tot[g]) {
-          const uint32_t v = (gw0 + 32u * g + wd) * 32u + nth_set_bit(bits, t - ex);
-          level[v] = lvl_next;
-          if (v < n_rows) deg = indptr[v + 1] - indptr[v];
+      for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u * kLgUnroll) {
+        uint32_t vv[kLgUnroll];
+#pragma unroll
+        for (int r = 0; r < kLgUnroll; r++) {
+          const uint32_t t = t0 + 32u * r + lane;
+          vv[r] = lg_vertex(newb[g], incl[g], tot[g], t, gw0 + 32u * g);
         }
-        w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
-        w_deg += __reduce_add_sync(kFull, deg);
+        uint32_t b[kLgUnroll], e[kLgUnroll];
+#pragma unroll
+        for (int r = 0; r < kLgUnroll; r++) {
+          b[r] = e[r] = 0;
+          if (vv[r] != kFull) {
+            level[vv[r]] = lvl_next;
+            if (vv[r] < n_rows) {
+              b[r] = indptr[vv[r]];
+              e[r] = indptr[vv[r] + 1];
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kLgUnroll; r++) {
+          const uint32_t deg = e[r] - b[r];
+          w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
+          w_deg += __reduce_add_sync(kFull, deg);
+        }
       }
     }
     // block-wide offsets: one atomic per block and step
@@ -478,30 +504,35 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
       // pass 2: write the kept entries in the same order
 #pragma unroll
       for (int g = 0; g < kLgGroups; g++) {
-        for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u) {
-          const uint32_t t = t0 + lane;
-          const uint32_t wd = lg_word_of(incl[g], t < tot[g] ? t : tot[g] - 1u);
-          const uint32_t bits = __shfl_sync(kFull, newb[g], wd);
-          const uint32_t ex = __shfl_sync(kFull, incl[g], wd) - __popc(bits);
-          uint32_t v = 0, b = 0, e = 0;
-          if (t < tot[g]) {
-            v = (gw0 + 32u * g + wd) * 32u + nth_set_bit(bits, t - ex);
-            if (v < n_rows) {
-              b = indptr[v];
-              e = indptr[v + 1];
+        for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u * kLgUnroll) {
+          uint32_t vv[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
+#pragma unroll
+          for (int r = 0; r < kLgUnroll; r++) {
+            const uint32_t t = t0 + 32u * r + lane;
+            vv[r] = lg_vertex(newb[g], incl[g], tot[g], t, gw0 + 32u * g);
+          }
+#pragma unroll
+          for (int r = 0; r < kLgUnroll; r++) {
+            b[r] = e[r] = 0;
+            if (vv[r] != kFull && vv[r] < n_rows) {
+              b[r] = indptr[vv[r]];
+              e[r] = indptr[vv[r] + 1];
             }
           }
-          const uint32_t deg = e - b;
-          const uint32_t km = __ballot_sync(kFull, deg > 0u);
-          const uint32_t dincl = warp_incl_scan(deg, lane);
-          if (deg) {
-            const uint32_t sl = slot + __popc(km & lt_mask);
-            qb[sl] = b;
-            qp[sl] = pref + dincl - deg;
-            qv[sl] = v;
+#pragma unroll
+          for (int r = 0; r < kLgUnroll; r++) {
+            const uint32_t deg = e[r] - b[r];
+            const uint32_t km = __ballot_sync(kFull, deg > 0u);
+            const uint32_t dincl = warp_incl_scan(deg, lane);
+            if (deg) {
+              const uint32_t sl = slot + __popc(km & lt_mask);
+              qb[sl] = b[r];
+              qp[sl] = pref + dincl - deg;
+              qv[sl] = vv[r];
+            }
+            slot += __popc(km);
+            pref += __shfl_sync(kFull, dincl, 31);
           }
-          slot += __popc(km);
-          pref += __shfl_sync(kFull, dincl, 31);
         }
       }
     }
@@ -615,23 +646,24 @@ __global__ void check_csc_kernel(const uint32_t *__restrict__ indptr,
 }
 
 // ---- kernel table ---------------------------------------------------------
-template <int U>
+template <int U, bool PAR>
 static const void *explore_fn_u(int arm) {
   switch (arm) {
-    case 0: return (const void *)explore_local_kernel<128, false, U>;
-    case 1: return (const void *)explore_local_kernel<256, false, U>;
-    case 2: return (const void *)explore_local_kernel<512, false, U>;
-    case 3: return (const void *)explore_global_kernel<128, U>;
-    case 4: return (const void *)explore_global_kernel<256, U>;
-    case 5: return (const void *)explore_global_kernel<512, U>;
-    case 6: return (const void *)explore_local_kernel<128, true, U>;
-    case 7: return (const void *)explore_local_kernel<256, true, U>;
-    case 8: return (const void *)explore_local_kernel<512, true, U>;
+    case 0: return (const void *)explore_local_kernel<128, false, U, PAR>;
+    case 1: return (const void *)explore_local_kernel<256, false, U, PAR>;
+    case 2: return (const void *)explore_local_kernel<512, false, U, PAR>;
+    case 3: return (const void *)explore_global_kernel<128, U, PAR>;
+    case 4: return (const void *)explore_global_kernel<256, U, PAR>;
+    case 5: return (const void *)explore_global_kernel<512, U, PAR>;
+    case 6: return (const void *)explore_local_kernel<128, true, U, PAR>;
+    case 7: return (const void *)explore_local_kernel<256, true, U, PAR>;
+    case 8: return (const void *)explore_local_kernel<512, true, U, PAR>;
     default: return nullptr;
   }
 }
-const void *explore_kernel_fn(int arm, int ipt) {
-  return ipt == 8 ? explore_fn_u<8>(arm) : explore_fn_u<4>(arm);
+const void *explore_kernel_fn(int arm, int ipt, bool parents) {
+  if (parents) return ipt == 8 ? explore_fn_u<8, true>(arm) : explore_fn_u<4, true>(arm);
+  return ipt == 8 ? explore_fn_u<8, false>(arm) : explore_fn_u<4, false>(arm);
 }
 const void *levelgen_kernel_fn() { return (const void *)levelgen_kernel<kLevelgenBlock>; }
 const void *init_kernel_fn() { return (const void *)init_kernel; }

@@ -18,7 +18,8 @@ inline uint32_t glb_chunk_edges(int ipt) { return 32u * (uint32_t)ipt * kGlbGrou
 // Kernel function pointers (for CUDA-graph kernel nodes and direct launches).
 // Every kernel takes (BfsDevState*) first; levelgen and init also take
 // (unsigned long long conditional_handle, int use_conditional).
-const void *explore_kernel_fn(int arm, int ipt);
+// parents: the variant that also records BFS-tree parents.
+const void *explore_kernel_fn(int arm, int ipt, bool parents);
 const void *levelgen_kernel_fn();
 const void *init_kernel_fn();
 const void *fill_kernel_fn();

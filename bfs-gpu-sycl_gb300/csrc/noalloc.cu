@@ -82,7 +82,7 @@ bfs_status setup_device(int dev) {
   int sms = 0, occ_ex = 0, occ_lg = 0;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, explore_kernel_fn(kArm, kIpt),
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, explore_kernel_fn(kArm, kIpt, false),
                                                       arm_block(kArm), 0);
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
@@ -176,7 +176,7 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
     NK(cudaStreamSynchronize(s));
     if (F == 0) break;
     void *ex_args[] = {&st};
-    NK(cudaLaunchKernel(explore_kernel_fn(kArm, kIpt), dim3(g_grid[dev][0]), dim3(arm_block(kArm)),
+    NK(cudaLaunchKernel(explore_kernel_fn(kArm, kIpt, false), dim3(g_grid[dev][0]), dim3(arm_block(kArm)),
                         ex_args, 0, s));
     void *lg_args[] = {&st, &no_cond, &zero};
     NK(cudaLaunchKernel(levelgen_kernel_fn(), dim3(g_grid[dev][1]), dim3(kLevelgenBlock), lg_args,

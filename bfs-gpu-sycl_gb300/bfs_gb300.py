@@ -137,6 +137,8 @@ def lib():
     _sig(L, "bfs_sched_attach", [VP, C.POINTER(C.c_float), C.c_float])
     _sig(L, "bfs_run_batch", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
                               C.POINTER(BatchStats)])
+    _sig(L, "bfs_run_batch_loop", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
+                                   C.c_int32, C.POINTER(BatchStats)])
     _sig(L, "bfs_multi_create", [C.c_uint32, C.POINTER(U32P), C.POINTER(U32P), U32P, U32P,
                                  C.POINTER(C.c_uint64), C.POINTER(VP)])
     _sig(L, "bfs_multi_free", [VP])
@@ -453,15 +455,18 @@ class Graph:
                                    C.byref(st) if st is not None else None))
         return st
 
-    def run_batch(self, roots, levels_ptr, want_edges=True):
+    def run_batch(self, roots, levels_ptr, want_edges=True, loop="graph"):
         """Multi-source BFS of len(roots) roots into a device int32 buffer of
-        len(roots) x n_cols; returns (edges uint64[len(roots)] or None, BatchStats)."""
+        len(roots) x n_cols; returns (edges uint64[len(roots)] or None, BatchStats).
+        loop="host" launches every kernel separately (for profilers)."""
         rt = np.ascontiguousarray(roots, np.uint32)
         ec = np.zeros(len(rt), np.uint64) if want_edges else None
         st = BatchStats()
-        check(lib().bfs_run_batch(self.h, rt.ctypes.data_as(U32P), len(rt), VP(levels_ptr),
-                                  ec.ctypes.data_as(C.POINTER(C.c_uint64)) if want_edges
-                                  else None, C.byref(st)))
+        check(lib().bfs_run_batch_loop(self.h, rt.ctypes.data_as(U32P), len(rt),
+                                       VP(levels_ptr),
+                                       ec.ctypes.data_as(C.POINTER(C.c_uint64)) if want_edges
+                                       else None,
+                                       LOOP_GRAPH if loop == "graph" else LOOP_HOST, C.byref(st)))
         return ec, st
 
     def sched_record(self, root, ipt=4, reps=3, max_levels=1 << 16):

@@ -340,6 +340,7 @@ struct MsWorkspace {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int grid_ex = 0, grid_lg = 0, grid_fill = 0;
+  size_t clear_bytes = 0;  // visited + next masks, cleared before each pass
 };
 
 namespace bfsgb {
@@ -396,6 +397,7 @@ static bfs_status ms_setup(bfs_graph *g) {
     s.qm[b] = (unsigned long long *)p; p += q8;
   }
   s.level_cap = g->n_cols + 1u;
+  w->clear_bytes = 2 * b64;
   int occ_ex = 0, occ_lg = 0;
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, (const void *)ms_explore_kernel,
                                                    kMsBlock, 0));
@@ -458,10 +460,45 @@ static bfs_status ms_setup(bfs_graph *g) {
   return BFS_OK;
 }
 
+// The same pass as the graph, driven from the host: one frontier-size read-back
+// per level.  Every kernel is a separate launch, which profilers can capture
+// (kernels inside a graph with a conditional node cannot be).
+static bfs_status ms_pass_host(bfs_graph *g, MsWorkspace *w) {
+  cudaStream_t s = g->stream;
+  MsState *st = w->d_st;
+  unsigned long long no_cond = 0;
+  int zero = 0;
+  MK(cudaMemsetAsync(w->mem, 0, w->clear_bytes, s));
+  ms_fill_kernel<<<w->grid_fill, 256, 0, s>>>(st);
+  MK(cudaGetLastError());
+  ms_init_kernel<<<1, kLanes, 0, s>>>(st, no_cond, zero);
+  MK(cudaGetLastError());
+  uint32_t *h_F = &w->h_st->F;
+  for (;;) {
+    MK(cudaMemcpyAsync(h_F, &st->F, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    MK(cudaStreamSynchronize(s));
+    if (*h_F == 0) break;
+    ms_explore_kernel<<<w->grid_ex, kMsBlock, 0, s>>>(st);
+    MK(cudaGetLastError());
+    ms_levelgen_kernel<<<w->grid_lg, kMsBlock, 0, s>>>(st, no_cond, zero);
+    MK(cudaGetLastError());
+  }
+  return BFS_OK;
+}
+
 extern "C" bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
                                     int32_t *levels_dev, uint64_t *edges_count_out,
                                     bfs_batch_stats *stats) {
+  return bfs_run_batch_loop(g, roots, n_roots, levels_dev, edges_count_out, BFS_LOOP_GRAPH,
+                            stats);
+}
+
+extern "C" bfs_status bfs_run_batch_loop(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                                         int32_t *levels_dev, uint64_t *edges_count_out,
+                                         int32_t loop, bfs_batch_stats *stats) {
   if (!g || !roots || !levels_dev) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  if (loop != BFS_LOOP_GRAPH && loop != BFS_LOOP_HOST)
+    return fail(BFS_ERR_INVALID_ARG, "loop must be BFS_LOOP_GRAPH or BFS_LOOP_HOST");
   for (uint32_t i = 0; i < n_roots; i++)
     if (roots[i] >= g->n_cols) return fail(BFS_ERR_ROOT, "root out of range");
   MK(cudaSetDevice(g->device));
@@ -482,7 +519,12 @@ extern "C" bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_
     for (uint32_t j = 0; j < nl; j++) s.roots[j] = roots[b0 + j];
     MK(cudaEventRecord(w->e0, g->stream));
     MK(cudaMemcpyAsync(w->d_st, w->h_st, sizeof(MsState), cudaMemcpyHostToDevice, g->stream));
-    MK(cudaGraphLaunch(w->exec, g->stream));
+    if (loop == BFS_LOOP_HOST) {
+      rc = ms_pass_host(g, w);
+      if (rc != BFS_OK) return rc;
+    } else {
+      MK(cudaGraphLaunch(w->exec, g->stream));
+    }
     MK(cudaEventRecord(w->e1, g->stream));
     MK(cudaMemcpyAsync(w->h_st, w->d_st, sizeof(MsState), cudaMemcpyDeviceToHost, g->stream));
     MK(cudaStreamSynchronize(g->stream));

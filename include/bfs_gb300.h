@@ -166,6 +166,12 @@ typedef struct bfs_batch_stats {
 bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
                          int32_t *levels_dev, uint64_t *edges_count_out,
                          bfs_batch_stats *stats);
+/* bfs_run_batch with the level loop chosen by loop (bfs_loop): BFS_LOOP_HOST
+ * launches every kernel separately (for profilers), BFS_LOOP_GRAPH is
+ * bfs_run_batch.  Same results either way. */
+bfs_status bfs_run_batch_loop(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                              int32_t *levels_dev, uint64_t *edges_count_out, int32_t loop,
+                              bfs_batch_stats *stats);
 
 /* ---- many small graphs in one launch ----------------------------------- */
 /* A batch of independent graphs (up to 2^18 vertices each) packed into one

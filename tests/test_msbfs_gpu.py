@@ -46,6 +46,11 @@ def test_partial_batches_duplicates_and_odd_roots(B, O):
     # a second call reuses the workspace
     ec2, _ = dg.run_batch(roots[:7], out.data_ptr())
     assert np.array_equal(out[:7].cpu().numpy(), ref[:7]) and np.array_equal(ec2, rec[:7])
+    # the host-driven level loop gives the same rows and counts
+    out.fill_(7)
+    ec3, st3 = dg.run_batch(roots, out.data_ptr(), loop="host")
+    assert st3.batches == 2 and st3.launches == st.launches
+    assert np.array_equal(out.cpu().numpy(), ref) and np.array_equal(ec3, rec)
     dg.free()
 
 

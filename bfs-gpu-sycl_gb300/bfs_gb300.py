@@ -126,6 +126,8 @@ def lib():
     _sig(L, "bfs_sample_roots", [U32P, C.c_uint32, C.c_uint32, C.c_uint64, U32P])
     _sig(L, "bfs_dataset_load", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost)])
     _sig(L, "bfs_dataset_write", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost)])
+    _sig(L, "bfs_dataset_write_split", [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(CscHost),
+                                        C.c_int32])
     _sig(L, "bfs_dataset_read_meta", [C.c_char_p, U32P, U32P, C.POINTER(C.c_uint64), U32P,
                                       C.c_uint32, U32P])
     _sig(L, "bfs_sched_record", [VP, C.c_uint32, C.c_int32, C.c_int32, C.POINTER(LevelSample),
@@ -228,10 +230,16 @@ def dataset_load(name, partitions=1, directory=None):
     return Csc._from_c(ch)
 
 
-def dataset_write(g, name, partitions=1, directory=None):
+SPLITS = {"balanced": 0, "nnz": 1, "row": 2}
+
+
+def dataset_write(g, name, partitions=1, directory=None, split="balanced"):
+    """Writes g as <directory>/<name>-csc-<partitions>/.  split: "balanced"
+    (in-degree balanced, exact rows) or the reference generator's "nnz" /
+    "row" splits with its round8 breaks (byte-identical files)."""
     ch = g._to_c()
-    check(lib().bfs_dataset_write(directory.encode() if directory else None, name.encode(),
-                                  partitions, C.byref(ch)))
+    check(lib().bfs_dataset_write_split(directory.encode() if directory else None,
+                                        name.encode(), partitions, C.byref(ch), SPLITS[split]))
 
 
 def dataset_read_meta(path, max_records=64):

@@ -8,6 +8,8 @@
 // Partition i holds the edges whose destination lies in its row range; every
 // partition has offsets for all columns.  A missing or empty file is an
 // error, like readFromMM (graph_load.hpp:23-48).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -86,6 +88,53 @@ bfs_status read_meta(const std::string &path, std::vector<MetaRec> *recs) {
   fclose(f);
   if (bad) return fail(BFS_ERR_IO, "error reading " + path);
   if (recs->empty()) return fail(BFS_ERR_IO, "no meta records in " + path);
+  return BFS_OK;
+}
+
+// Destination-row breaks of scripts/generator.py, computed the way numpy and
+// scipy compute them there, so that the files come out byte-identical:
+//   nnzSplit (:22-40): cum = inclusive prefix of row nnz (in-degree);
+//     targets = np.arange(0, total, total / P) -- ceil(total / step) values
+//     i * step in float64; break = first row with cum >= target
+//     (np.searchsorted, side 'left'); then the row count appended.
+//   rowSplit (:42-54): step = int(alignedIncrement(rows / P, 0, 64)), the
+//     float quotient rounded up to a multiple of 64 (:249-254); breaks =
+//     np.arange(0, rows, step) plus the row count -- fewer than P partitions
+//     when step * (P - 1) >= rows.
+// Every break is then round8'ed, (x + 4) & ~7 (:11-12), and a partition is
+// the row slice [min(lo, rows), min(hi, rows)) (slicing past the end of the
+// matrix clips), so the last rows are dropped when round8(rows) < rows.
+bfs_status reference_breaks(int32_t split, uint32_t parts, const std::vector<uint64_t> &indeg,
+                            std::vector<uint32_t> *brk) {
+  const uint64_t rows = indeg.size();
+  std::vector<uint64_t> b;
+  if (split == BFS_SPLIT_REF_NNZ) {
+    std::vector<uint64_t> cum(rows);
+    uint64_t run = 0;
+    for (uint64_t r = 0; r < rows; r++) cum[r] = run += indeg[r];
+    if (run == 0) return fail(BFS_ERR_INVALID_ARG, "the reference's nnz split needs edges");
+    const double step = (double)run / (double)parts;
+    const uint64_t len = (uint64_t)std::ceil((double)run / step);
+    for (uint64_t i = 0; i < len; i++) {
+      const double t = (double)i * step;
+      uint64_t lo = 0, hi = rows;  // first r with (double)cum[r] >= t
+      while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if ((double)cum[mid] < t) lo = mid + 1; else hi = mid;
+      }
+      b.push_back(lo);
+    }
+  } else {
+    if (rows == 0) return fail(BFS_ERR_INVALID_ARG, "the reference's row split needs rows");
+    double res = (double)rows / (double)parts;
+    const double rem = std::fmod(res, 64.0);
+    if (rem != 0.0) res += 64.0 - rem;
+    const uint64_t step = (uint64_t)res;
+    for (uint64_t x = 0; x < rows; x += step) b.push_back(x);
+  }
+  b.push_back(rows);
+  brk->clear();
+  for (uint64_t x : b) brk->push_back((uint32_t)std::min<uint64_t>((x + 4) & ~7ull, rows));
   return BFS_OK;
 }
 
@@ -179,8 +228,15 @@ bfs_status bfs_dataset_load(const char *dir, const char *name, uint32_t partitio
 
 bfs_status bfs_dataset_write(const char *dir, const char *name, uint32_t partitions,
                              const bfs_csc_host *g) {
+  return bfs_dataset_write_split(dir, name, partitions, g, BFS_SPLIT_BALANCED);
+}
+
+bfs_status bfs_dataset_write_split(const char *dir, const char *name, uint32_t partitions,
+                                   const bfs_csc_host *g, int32_t split) {
   if (!name || !g || !g->indptr || (!g->inds && g->nnz) || partitions < 1 || partitions > 64)
     return fail(BFS_ERR_INVALID_ARG, "bad dataset arguments");
+  if (split != BFS_SPLIT_BALANCED && split != BFS_SPLIT_REF_NNZ && split != BFS_SPLIT_REF_ROW)
+    return fail(BFS_ERR_INVALID_ARG, "unknown split mode");
   const uint32_t n = g->n_cols;
   const std::string pre = part_prefix(dir, name, partitions);
   const std::string folder = pre.substr(0, pre.rfind('/'));
@@ -199,9 +255,10 @@ bfs_status bfs_dataset_write(const char *dir, const char *name, uint32_t partiti
     if (g->inds[k] >= n) return fail(BFS_ERR_GRAPH, "destination id >= cols");
     indeg[g->inds[k]]++;
   }
-  std::vector<uint32_t> brk(partitions + 1, 0);
-  brk[partitions] = g->n_rows;
-  {
+  std::vector<uint32_t> brk;
+  if (split == BFS_SPLIT_BALANCED) {
+    brk.assign(partitions + 1, 0);
+    brk[partitions] = g->n_rows;
     uint64_t run = 0;
     uint32_t p = 1;
     for (uint32_t r = 0; r < g->n_rows && p < partitions; r++) {
@@ -209,15 +266,23 @@ bfs_status bfs_dataset_write(const char *dir, const char *name, uint32_t partiti
       run += indeg[r];
     }
     while (p < partitions) brk[p++] = g->n_rows;
+  } else {
+    bfs_status rc = reference_breaks(split, partitions, indeg, &brk);
+    if (rc != BFS_OK) return rc;
   }
-  std::vector<unsigned char> meta(20 * (size_t)partitions);
-  for (uint32_t p = 0; p < partitions; p++) {
+  const uint32_t n_parts = (uint32_t)brk.size() - 1;
+  // the balanced split keeps every edge in a single partition (rows may be
+  // fewer than cols); the reference's splits keep only destinations inside
+  // the (round8-clipped) row range, also for P = 1
+  const bool keep_all = split == BFS_SPLIT_BALANCED && partitions == 1;
+  std::vector<unsigned char> meta(20 * (size_t)n_parts);
+  for (uint32_t p = 0; p < n_parts; p++) {
     const uint32_t lo = brk[p], hi = brk[p + 1];
     std::vector<uint32_t> ip((size_t)n + 1, 0), ix;
     for (uint32_t v = 0; v < n; v++) {
       for (uint32_t k = g->indptr[v]; k < g->indptr[v + 1]; k++) {
         const uint32_t d = g->inds[k];
-        if (partitions == 1 || (d >= lo && d < hi)) ix.push_back(d);
+        if (keep_all || (d >= lo && d < hi)) ix.push_back(d);
       }
       ip[v + 1] = (uint32_t)ix.size();
     }

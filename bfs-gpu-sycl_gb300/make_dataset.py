@@ -2,8 +2,14 @@
 
 Counterpart of scripts/genGraph.py + scripts/generator.py: produces
 <dir>/<name>-csc-<P>/<name>-csc-{meta,<i>-indptr,<i>-inds}.bin for one or more
-partition counts P (destination rows split by in-degree, like nnzSplit,
-generator.py:22-40, without its round-to-8 of the breaks).
+partition counts P.  --split picks the destination-row breaks:
+  balanced (default)  in-degree balanced, exact row counts, every edge kept
+  nnz | row           the reference generator's nnzSplit / rowSplit with its
+                      round8 breaks (generator.py:11-54): the same files it
+                      writes, byte for byte, including its quirks (the last
+                      rows dropped when round8 rounds down, empty partitions,
+                      fewer than P partitions from the row split); the default
+                      name gets the reference's -nnz / -row suffix
 
 Sources:
   rmat SCALE EF    seeded R-MAT (a/b/c/d .57/.19/.19/.05), deduplicated, no
@@ -18,6 +24,8 @@ Sources:
 Examples:
   python bfs-gpu-sycl_gb300/make_dataset.py rmat 19 16 --partitions 1 2 4
   python bfs-gpu-sycl_gb300/make_dataset.py edgelist my.txt --name my-graph
+  python bfs-gpu-sycl_gb300/make_dataset.py edgelist my.txt --split nnz \
+      --partitions 1 2 3 4 5 6 7 8        # like: generator.py my nnz
 """
 import argparse
 import os
@@ -65,6 +73,7 @@ def main(argv=None):
     ap.add_argument("--partitions", type=int, nargs="+", default=[1])
     ap.add_argument("--dir", default=os.path.join(os.getcwd(), "dataset"))
     ap.add_argument("--name", default=None)
+    ap.add_argument("--split", choices=["balanced", "nnz", "row"], default="balanced")
     a = ap.parse_args(argv)
     if a.kind == "rmat":
         scale, ef = int(a.args[0]), int(a.args[1])
@@ -81,8 +90,10 @@ def main(argv=None):
     else:
         g = csc_from_edgelist(a.args[0], a.dim)
         name = a.name or os.path.splitext(os.path.basename(a.args[0]))[0]
+    if a.split != "balanced" and not a.name:
+        name += "-" + a.split
     for p in a.partitions:
-        B.dataset_write(g, name, p, a.dir)
+        B.dataset_write(g, name, p, a.dir, split=a.split)
         print(f"{a.dir}/{name}-csc-{p}: {g.n_cols} vertices, {g.nnz} edges, {p} partition(s)")
 
 

@@ -323,10 +323,24 @@ bfs_status bfs_sample_roots(const uint32_t *indptr, uint32_t n_rows, uint32_t co
 bfs_status bfs_dataset_load(const char *dir, const char *name, uint32_t partitions,
                             bfs_csc_host *out);
 /* Writes a single- or multi-partition dataset in the same layout (the
- * inverse of the above; nnz-balanced row split for P > 1 like
- * scripts/generator.py:22-40, without its round-to-8 of the breaks). */
+ * inverse of the above; in-degree balanced destination-row split for P > 1,
+ * exact row counts: bfs_dataset_write_split with BFS_SPLIT_BALANCED). */
 bfs_status bfs_dataset_write(const char *dir, const char *name, uint32_t partitions,
                              const bfs_csc_host *g);
+/* Destination-row split of bfs_dataset_write_split. */
+typedef enum bfs_split {
+  BFS_SPLIT_BALANCED = 0, /* in-degree balanced, exact rows, all edges kept at P = 1 */
+  BFS_SPLIT_REF_NNZ = 1,  /* scripts/generator.py nnzSplit + round8 (:11-40) */
+  BFS_SPLIT_REF_ROW = 2   /* scripts/generator.py rowSplit + round8 (:11-12, :42-54) */
+} bfs_split;
+/* bfs_dataset_write with the split chosen by split (bfs_split).  The two
+ * reference modes write the files scripts/generator.py writes for the same
+ * (square, duplicate-free, column-sorted) matrix byte for byte, quirks
+ * included: round8 of the last break drops the last rows when it rounds
+ * down, partitions can be empty, and the row split can write fewer than P
+ * partitions (the folder is still named -csc-<P>). */
+bfs_status bfs_dataset_write_split(const char *dir, const char *name, uint32_t partitions,
+                                   const bfs_csc_host *g, int32_t split);
 /* Reads only the meta records (20 bytes each: u32 rows, u32 cols, u64 nnz,
  * u32 startRow; src/graph_load.hpp:49-92).  Returns the record count in
  * *count (at most max_records are stored). */

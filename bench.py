@@ -290,19 +290,23 @@ def run_gb300(a):
         except Exception:
             traffic = None
 
-    # per-arm table (GTEPS of every explore form x block size, graph loop)
+    # per-arm table (GTEPS of every explore form x block size, graph loop),
+    # with the learned schedule on the same roots for a like-for-like row
     arms = {}
     if not a.skip_arms:
-        for lb in ("llb", "glb", "slb"):
-            for blk in (128, 256, 512):
-                o = B.options(lb, blk)
-                dg.run_device(int(roots[0]), lv.data_ptr(), opts=o)
-                ms, ed = 0.0, 0.0
-                for r in roots[a.warmup:a.warmup + 4]:
-                    st = dg.run_device(int(r), lv.data_ptr(), opts=o)
-                    ms += st.device_ms
-                    ed += st.edges_count
-                arms[f"{lb}{blk}"] = round(ed / (ms * 1e-3) / 1e9, 3)
+        plans = [(lb, blk) for lb in ("llb", "glb", "slb") for blk in (128, 256, 512)]
+        if weights is not None:
+            plans.append(("learned", 256))
+        for lb, blk in plans:
+            o = B.options(lb, blk)
+            dg.run_device(int(roots[0]), lv.data_ptr(), opts=o)
+            ms, ed = 0.0, 0.0
+            for r in roots[a.warmup:a.warmup + 4]:
+                st = dg.run_device(int(r), lv.data_ptr(), opts=o)
+                ms += st.device_ms
+                ed += st.edges_count
+            arms["learned" if lb == "learned" else f"{lb}{blk}"] = \
+                round(ed / (ms * 1e-3) / 1e9, 3)
 
     # batched: multi-source passes of 64 roots vs 64 sequential runs.
     # (1) the batched configuration: RMAT-22/EF16 seed 6, 1024 seeded roots in

@@ -221,8 +221,8 @@ static bfs_status check_dims(uint32_t n_rows, uint32_t n_cols, uint64_t nnz) {
   if (n_cols == 0) return fail(BFS_ERR_INVALID_ARG, "n_cols must be > 0");
   if (n_rows > n_cols) return fail(BFS_ERR_INVALID_ARG, "n_rows must be <= n_cols");
   if (n_cols > 0xFFFFF000u) return fail(BFS_ERR_INVALID_ARG, "n_cols too large");
-  if (nnz > 0xFFFFFFFFull)
-    return fail(BFS_ERR_INVALID_ARG, "nnz must fit the uint32 CSC offsets");
+  if (nnz > BFS_MAX_EDGES)
+    return fail(BFS_ERR_INVALID_ARG, "nnz must be <= BFS_MAX_EDGES (2^32 - 4096)");
   return BFS_OK;
 }
 

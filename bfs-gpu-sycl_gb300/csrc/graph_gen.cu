@@ -121,8 +121,8 @@ bfs_status build_csc(uint32_t n, uint64_t m, bool symmetrize, EdgeFn edge,
   });
   uint64_t nnz = 0;
   for (uint32_t v = 0; v < n; v++) nnz += cnt[v];
-  if (nnz > 0xFFFFFFFFull)
-    return fail(BFS_ERR_UNSUPPORTED, "graph has more than 2^32-1 edges");
+  if (nnz > BFS_MAX_EDGES)
+    return fail(BFS_ERR_UNSUPPORTED, "graph has more than BFS_MAX_EDGES edges");
   out->n_rows = out->n_cols = n;
   out->nnz = nnz;
   out->indptr = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)n + 1));
@@ -335,8 +335,8 @@ bfs_status bfs_gen_rmat_device(uint32_t scale, uint32_t edge_factor, double a,
                 "tail copy");
       if (last == (1ull << bits) - 1ull) nnz--;
     }
-    if (nnz > 0xFFFFFFFFull) {
-      rc = fail(BFS_ERR_UNSUPPORTED, "graph has more than 2^32-1 edges");
+    if (nnz > BFS_MAX_EDGES) {
+      rc = fail(BFS_ERR_UNSUPPORTED, "graph has more than BFS_MAX_EDGES edges");
       goto done;
     }
     GEN_CHECK(cudaMalloc(&indptr, sizeof(uint32_t) * ((size_t)n + 1)), "indptr");

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     explore_local_kernel(BfsDevState *__restrict__ st) {
   constexpr int NW = B / 32;
   __shared__ uint32_t s_off[B + 1];
-  __shared__ uint32_t s_beg[B];
+  __shared__ uint32_t s_dif[B];  // first edge - tile offset, mod 2^32
   __shared__ uint32_t s_vid[B];
   __shared__ uint32_t s_wsum[NW];
 
@@ -187,8 +187,9 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     }
     __syncthreads();
     const uint32_t total = s_wsum[NW - 1];
-    s_off[threadIdx.x] = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
-    s_beg[threadIdx.x] = beg;
+    const uint32_t off = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
+    s_off[threadIdx.x] = off;
+    s_dif[threadIdx.x] = beg - off;
     if (PAR) s_vid[threadIdx.x] = vid;
     if (threadIdx.x == 0) s_off[B] = total;
     __syncthreads();
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
           addr[u] = kFull;
           from[u] = 0;
           if (e < w1) {
-            addr[u] = s_beg[o] + (e - s_off[o]);
+            addr[u] = e + s_dif[o];
             if (PAR) from[u] = s_vid[o];
           }
           cur = __shfl_sync(kFull, o, 31);
@@ -274,53 +275,92 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
   for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
     const uint32_t w0 = c * CHUNK;  // < EF, no overflow
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
+    // An entry's edge e lives at inds[e + (qb - qp)]: one difference per
+    // entry (mod 2^32) instead of its start and first edge, so a lane needs
+    // one shuffle per round to address its edge.  Shuffles and warp
+    // reductions use the same L1 data pipe as the bitmap probes.
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
-    uint32_t cur_start = qp[cur], cur_beg = qb[cur];
+    uint32_t cur_d = qb[cur] - qp[cur];
     uint32_t cur_vid = PAR ? qv[cur] : 0u;
-    // starts / first edges / ids of the 32 entries after cur; reloaded only
-    // when the owner of the last lane moves past cur
-    uint32_t j = cur + 1u + lane;
-    uint32_t bnd = (j <= F) ? qp[j] : kFull;  // qp[F] = EF
-    uint32_t bg = (j < F) ? qb[j] : 0u;
-    uint32_t vd = (PAR && j < F) ? qv[j] : 0u;
-    for (uint32_t base = w0; base < w1; base += kRound) {
-      uint32_t addr[U], from[U];
+    // Window: starts / differences / ids of entries c0 + 1 .. c0 + 32, one
+    // per lane.  It serves every round whose starts all lie inside it, i.e.
+    // while the start of entry c0 + 32 is >= the round's last edge; only
+    // then is it re-based at cur (about once per 32 entries, not per round).
+    uint32_t c0 = cur;
+    uint32_t bnd = (c0 + 1u + lane <= F) ? qp[c0 + 1u + lane] : kFull;  // qp[F] = EF
+    uint32_t dl = (c0 + 1u + lane < F) ? qb[c0 + 1u + lane] - bnd : 0u;
+    uint32_t vd = (PAR && c0 + 1u + lane < F) ? qv[c0 + 1u + lane] : 0u;
+    uint32_t wlast = __shfl_sync(kFull, bnd, 31);
+    // Edge addresses of the U rounds starting at edge `base`.
+    auto resolve = [&](uint32_t base, uint32_t (&ad)[U], uint32_t (&fr)[U]) {
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
         const uint32_t e = rb + lane;
+        if (wlast < rb || wlast - rb < 31u) {  // warp-uniform
+          c0 = cur;
+          const uint32_t j = c0 + 1u + lane;
+          bnd = (j <= F) ? qp[j] : kFull;
+          dl = (j < F) ? qb[j] - bnd : 0u;
+          vd = (PAR && j < F) ? qv[j] : 0u;
+          wlast = __shfl_sync(kFull, bnd, 31);
+        }
+        // entries at or before cur have starts < rb: p wraps past 32
         const uint32_t p = bnd - rb;
         const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
         const uint32_t k = __popc(starts & ((2u << lane) - 1u));
-        const uint32_t srcl = k ? k - 1u : 0u;
-        const uint32_t s_start = __shfl_sync(kFull, bnd, srcl);
-        const uint32_t s_beg = __shfl_sync(kFull, bg, srcl);
+        // entry cur + k sits in lane cur + k - c0 - 1 of the window
+        const uint32_t srcl = k ? cur + k - c0 - 1u : 0u;
+        const uint32_t s_d = __shfl_sync(kFull, dl, srcl);
         const uint32_t s_vid = PAR ? __shfl_sync(kFull, vd, srcl) : 0u;
-        addr[u] = kFull;
-        from[u] = 0;
+        ad[u] = kFull;
+        fr[u] = 0;
         if (e < w1) {
-          addr[u] = (k ? s_beg : cur_beg) + (e - (k ? s_start : cur_start));
-          if (PAR) from[u] = k ? s_vid : cur_vid;
+          ad[u] = e + (k ? s_d : cur_d);
+          if (PAR) fr[u] = k ? s_vid : cur_vid;
         }
-        // carry the owner of lane 31 into the next round
-        const uint32_t k31 = __shfl_sync(kFull, k, 31);
+        // the owner of lane 31 is entry cur + popc(starts)
+        const uint32_t k31 = __popc(starts);
         if (k31) {
           cur += k31;
-          cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
-          cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
-          if (PAR) cur_vid = __shfl_sync(kFull, vd, k31 - 1u);
-          j = cur + 1u + lane;
-          bnd = (j <= F) ? qp[j] : kFull;
-          bg = (j < F) ? qb[j] : 0u;
-          vd = (PAR && j < F) ? qv[j] : 0u;
+          cur_d = __shfl_sync(kFull, dl, cur - c0 - 1u);
+          if (PAR) cur_vid = __shfl_sync(kFull, vd, cur - c0 - 1u);
         }
       }
-      uint32_t nb[U];
+    };
+    // Software pipeline: the edge loads of the next U rounds are issued
+    // before the bitmap probes of the current ones, so the probes' latency
+    // covers them.
+    uint32_t nb[U], from[U];
+    {
+      uint32_t ad[U];
+      resolve(w0, ad, from);
 #pragma unroll
-      for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
+      for (int u = 0; u < U; u++) nb[u] = ad[u] != kFull ? ld_stream(inds + ad[u], pol) : kFull;
+    }
+    for (uint32_t base = w0; base < w1; base += kRound) {
+      uint32_t nb2[U], from2[U];
+      if (base + kRound < w1) {  // warp-uniform; no overflow: w1 <= EF < 2^32 - kRound
+        uint32_t ad[U];
+        resolve(base + kRound, ad, from2);
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          nb2[u] = ad[u] != kFull ? ld_stream(inds + ad[u], pol) : kFull;
+      } else {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          nb2[u] = kFull;
+          from2[u] = 0;
+        }
+      }
 #pragma unroll
       for (int u = 0; u < U; u++)
-        if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
+        if (nb[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        nb[u] = nb2[u];
+        from[u] = from2[u];
+      }
     }
   }
 }
@@ -357,64 +397,31 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
 }
 
-// Level generation.  Blocks claim spans of NW * kLgGroups * 32 bitmap words
-// from a counter (dense regions of the bitmap are uneven), and a warp owns
-// kLgGroups groups of 32 words of the span.  In each group the new vertices (vis & ~prev) are processed
-// flattened: lane l of round r takes the (32 r + l)-th new vertex of the
-// group, so 32 indptr loads are in flight per round whatever the bit layout.
-// Pass 1 writes levels and counts kept entries and their degrees; one atomic
-// per block and step reserves queue slots and edge offsets; pass 2 re-reads
-// the (now cached) indptr pairs and writes the entries.
-constexpr int kLgGroups = 2;
-
-// Word (0..31) holding the t-th new vertex of a group, given each lane's
-// inclusive prefix of per-word new counts (binary search over the lanes).
-__device__ __forceinline__ uint32_t lg_word_of(uint32_t incl, uint32_t t) {
-  uint32_t lo = 0, hi = 31;  // the answer is <= 31 because t < incl of lane 31
-#pragma unroll
-  for (int s = 0; s < 5; s++) {
-    const uint32_t mid = (lo + hi) >> 1;
-    const uint32_t im = __shfl_sync(kFull, incl, mid);
-    if (im <= t) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
-// Position (0..31) of the set bit of rank n (0-based) in x, for n < popc(x):
-// the smallest p with popc(x & bits[0..p]) > n.
-__device__ __forceinline__ uint32_t nth_set_bit(uint32_t x, uint32_t n) {
-  uint32_t lo = 0, hi = 31;
-#pragma unroll
-  for (int s = 0; s < 5; s++) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if ((uint32_t)__popc(x & ((2u << mid) - 1u)) > n) hi = mid; else lo = mid + 1;
-  }
-  return lo;
-}
-
+// Level generation.  Blocks claim spans of NW * 32 bitmap words from a
+// counter (the density of new vertices is uneven over the bitmap); warp w of
+// a block owns the w-th group of 32 words of its span.  A warp first lists
+// its group's new vertices (vis & ~prev) in shared memory -- each lane walks
+// its word's set bits -- so that lane l of round r then takes the
+// (32 r + l)-th new vertex with one shared load, and 32 indptr loads are in
+// flight per round whatever the bit layout.  Pass 1 writes levels and counts
+// kept entries and their degrees; thread 0 reserves the block's queue slots
+// and edge offsets with one atomic and claims the block's next span in the
+// same step; pass 2 re-reads the (now cached) indptr pairs and writes the
+// entries.  Two block barriers per span.
 constexpr int kLgUnroll = 4;
-
-// Vertex of the t-th new bit of a group of 32 words starting at word w0, or
-// kFull when t is past the group's total (all lanes take part: shuffles).
-__device__ __forceinline__ uint32_t lg_vertex(uint32_t newb, uint32_t incl, uint32_t tot,
-                                              uint32_t t, uint32_t w0) {
-  const uint32_t wd = lg_word_of(incl, t < tot ? t : (tot ? tot - 1u : 0u));
-  const uint32_t bits = __shfl_sync(kFull, newb, wd);
-  const uint32_t ex = __shfl_sync(kFull, incl, wd) - __popc(bits);
-  if (t >= tot) return kFull;
-  return (w0 + wd) * 32u + nth_set_bit(bits, t - ex);
-}
+constexpr int kLgMinBlocks = 5;  // 1280 threads per SM: at most 48 registers
 
 template <int B>
-__global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ st,
-                                                     unsigned long long cond,
-                                                     int use_cond) {
+__global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *__restrict__ st,
+                                                                   unsigned long long cond,
+                                                                   int use_cond) {
   constexpr int NW = B / 32;
-  constexpr uint32_t kSpan = 32u * kLgGroups;  // words per warp and step
+  constexpr uint32_t kSpan = NW * 32u;  // words per block and step
+  __shared__ uint32_t s_list[NW][32 * 32];
   __shared__ unsigned long long s_wtot[NW];
   __shared__ unsigned long long s_base;
+  __shared__ uint32_t s_sb[2];
   __shared__ uint32_t s_reached[NW];
-  __shared__ uint32_t s_sb;
   __shared__ int s_last;
 
   const uint32_t words = st->words;
@@ -430,62 +437,59 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
   uint32_t *__restrict__ qv = st->qv[nq];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t *__restrict__ list = s_list[warp];
   uint32_t reached = 0;
 
-  for (;;) {
-    if (threadIdx.x == 0) s_sb = atomicAdd(&st->lg_cursor, NW * kSpan);
-    __syncthreads();
-    const uint32_t sb = s_sb;
+  if (threadIdx.x == 0) s_sb[0] = atomicAdd(&st->lg_cursor, kSpan);
+  __syncthreads();
+  for (uint32_t step = 0;; step ^= 1u) {
+    const uint32_t sb = s_sb[step];
     if (sb >= words) break;
-    const uint32_t gw0 = sb + warp * kSpan;  // first word of this warp's span
-    uint32_t newb[kLgGroups], incl[kLgGroups], tot[kLgGroups];
-#pragma unroll
-    for (int g = 0; g < kLgGroups; g++) {
-      const uint32_t w = gw0 + 32u * g + lane;
-      uint32_t nb = 0;
-      if (gw0 + 32u * g < words) {  // words is a multiple of 32
-        const uint32_t vw = V[w], pw = P[w];
-        nb = vw & ~pw;
-        if (nb) P[w] = vw;
+    const uint32_t w0 = sb + warp * 32u;  // words is a multiple of 32
+    uint32_t tot = 0;
+    if (w0 < words) {
+      const uint32_t vw = V[w0 + lane], pw = P[w0 + lane];
+      uint32_t x = vw & ~pw;
+      if (x) P[w0 + lane] = vw;
+      const uint32_t c = __popc(x);
+      const uint32_t incl = warp_incl_scan(c, lane);
+      tot = __shfl_sync(kFull, incl, 31);
+      uint32_t pos = incl - c;
+      const uint32_t vbase = (w0 + lane) * 32u;
+      __syncwarp();  // the previous span's reads of the list are done
+      while (x) {
+        list[pos++] = vbase + (uint32_t)(__ffs(x) - 1);
+        x &= x - 1u;
       }
-      newb[g] = nb;
-      reached += __popc(nb);
-      incl[g] = warp_incl_scan(__popc(nb), lane);
-      tot[g] = __shfl_sync(kFull, incl[g], 31);
+      __syncwarp();
     }
+    reached += tot;
     // pass 1: levels; kept-entry count and degree sum of the warp.  kLgUnroll
     // rounds are resolved first so their indptr loads are in flight together.
     uint32_t w_cnt = 0, w_deg = 0;
+    for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
+      uint32_t b[kLgUnroll], e[kLgUnroll];
 #pragma unroll
-    for (int g = 0; g < kLgGroups; g++) {
-      for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u * kLgUnroll) {
-        uint32_t vv[kLgUnroll];
-#pragma unroll
-        for (int r = 0; r < kLgUnroll; r++) {
-          const uint32_t t = t0 + 32u * r + lane;
-          vv[r] = lg_vertex(newb[g], incl[g], tot[g], t, gw0 + 32u * g);
-        }
-        uint32_t b[kLgUnroll], e[kLgUnroll];
-#pragma unroll
-        for (int r = 0; r < kLgUnroll; r++) {
-          b[r] = e[r] = 0;
-          if (vv[r] != kFull) {
-            level[vv[r]] = lvl_next;
-            if (vv[r] < n_rows) {
-              b[r] = indptr[vv[r]];
-              e[r] = indptr[vv[r] + 1];
-            }
+      for (int r = 0; r < kLgUnroll; r++) {
+        const uint32_t t = t0 + 32u * r + lane;
+        b[r] = e[r] = 0;
+        if (t < tot) {
+          const uint32_t v = list[t];
+          level[v] = lvl_next;
+          if (v < n_rows) {
+            b[r] = indptr[v];
+            e[r] = indptr[v + 1];
           }
         }
+      }
 #pragma unroll
-        for (int r = 0; r < kLgUnroll; r++) {
-          const uint32_t deg = e[r] - b[r];
-          w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
-          w_deg += __reduce_add_sync(kFull, deg);
-        }
+      for (int r = 0; r < kLgUnroll; r++) {
+        const uint32_t deg = e[r] - b[r];
+        w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
+        w_deg += __reduce_add_sync(kFull, deg);
       }
     }
-    // block-wide offsets: one atomic per block and step
+    // block-wide offsets (one atomic per block and step) and the next span
     if (lane == 0) s_wtot[warp] = ((unsigned long long)w_cnt << 32) | w_deg;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -496,51 +500,46 @@ __global__ void __launch_bounds__(B) levelgen_kernel(BfsDevState *__restrict__ s
         run += x;
       }
       s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
+      s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
     }
     __syncthreads();
     if (w_cnt) {
-      unsigned long long wb = s_base + s_wtot[warp];
+      const unsigned long long wb = s_base + s_wtot[warp];
       uint32_t slot = (uint32_t)(wb >> 32), pref = (uint32_t)wb;
       // pass 2: write the kept entries in the same order
+      for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
+        uint32_t vv[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
 #pragma unroll
-      for (int g = 0; g < kLgGroups; g++) {
-        for (uint32_t t0 = 0; t0 < tot[g]; t0 += 32u * kLgUnroll) {
-          uint32_t vv[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
-#pragma unroll
-          for (int r = 0; r < kLgUnroll; r++) {
-            const uint32_t t = t0 + 32u * r + lane;
-            vv[r] = lg_vertex(newb[g], incl[g], tot[g], t, gw0 + 32u * g);
+        for (int r = 0; r < kLgUnroll; r++) {
+          const uint32_t t = t0 + 32u * r + lane;
+          vv[r] = t < tot ? list[t] : kFull;
+          b[r] = e[r] = 0;
+          if (vv[r] < n_rows) {  // kFull >= n_rows
+            b[r] = indptr[vv[r]];
+            e[r] = indptr[vv[r] + 1];
           }
+        }
 #pragma unroll
-          for (int r = 0; r < kLgUnroll; r++) {
-            b[r] = e[r] = 0;
-            if (vv[r] != kFull && vv[r] < n_rows) {
-              b[r] = indptr[vv[r]];
-              e[r] = indptr[vv[r] + 1];
-            }
+        for (int r = 0; r < kLgUnroll; r++) {
+          const uint32_t deg = e[r] - b[r];
+          const uint32_t km = __ballot_sync(kFull, deg > 0u);
+          const uint32_t dincl = warp_incl_scan(deg, lane);
+          if (deg) {
+            const uint32_t sl = slot + __popc(km & lt_mask);
+            qb[sl] = b[r];
+            qp[sl] = pref + dincl - deg;
+            qv[sl] = vv[r];
           }
-#pragma unroll
-          for (int r = 0; r < kLgUnroll; r++) {
-            const uint32_t deg = e[r] - b[r];
-            const uint32_t km = __ballot_sync(kFull, deg > 0u);
-            const uint32_t dincl = warp_incl_scan(deg, lane);
-            if (deg) {
-              const uint32_t sl = slot + __popc(km & lt_mask);
-              qb[sl] = b[r];
-              qp[sl] = pref + dincl - deg;
-              qv[sl] = vv[r];
-            }
-            slot += __popc(km);
-            pref += __shfl_sync(kFull, dincl, 31);
-          }
+          slot += __popc(km);
+          pref += __shfl_sync(kFull, dincl, 31);
         }
       }
     }
-    __syncthreads();
+    // the list is rewritten only after the next step's first barrier, so
+    // pass 2 needs no trailing barrier
   }
 
-  // reached-vertex count: one atomic per block
-  reached = __reduce_add_sync(kFull, reached);
+  // reached-vertex count: one atomic per block (reached is warp-uniform)
   if (lane == 0) s_reached[warp] = reached;
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -286,7 +286,7 @@ bfs_status bfs_multi_create(uint32_t n_graphs, const uint32_t *const *indptrs,
   uint64_t vb = 0, eb = 0, lb = 0;
   for (uint32_t g = 0; g < n_graphs; g++) {
     if (!indptrs[g] || (!inds[g] && nnz[g]) || n_cols[g] == 0 || n_rows[g] > n_cols[g] ||
-        n_cols[g] > kMultiMaxVertices || nnz[g] > 0xFFFFFFFFull || indptrs[g][n_cols[g]] != nnz[g]) {
+        n_cols[g] > kMultiMaxVertices || nnz[g] > BFS_MAX_EDGES || indptrs[g][n_cols[g]] != nnz[g]) {
       delete m;
       return fail(BFS_ERR_INVALID_ARG, "graph " + std::to_string(g) +
                                            ": bad sizes (at most 2^18 vertices per graph)");

@@ -119,7 +119,7 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
     return fail(BFS_ERR_INVALID_ARG,
                 "bfs_run_device_noalloc supports at most " + std::to_string(kMaxV) +
                     " vertices (its fixed scratch size); use bfs_run_device for larger graphs");
-  if (nnz > 0xFFFFFFFFull) return fail(BFS_ERR_INVALID_ARG, "nnz must fit uint32 offsets");
+  if (nnz > BFS_MAX_EDGES) return fail(BFS_ERR_INVALID_ARG, "nnz must be <= BFS_MAX_EDGES");
   if (root >= n_cols) return fail(BFS_ERR_ROOT, "root out of range");
   int dev = 0;
   NK(cudaGetDevice(&dev));

@@ -81,6 +81,9 @@ typedef struct bfs_options {
 } bfs_options;
 
 #define BFS_MAX_RECORDED_LEVELS 4096
+/* Largest edge count a device graph may have: the kernels walk edge offsets
+ * in uint32 with whole 128-edge steps, which must not wrap. */
+#define BFS_MAX_EDGES 0xFFFFF000u
 
 typedef struct bfs_stats {
   uint64_t edges_count;   /* sum of out-degrees of expanded vertices; the

@@ -109,10 +109,20 @@ struct BfsDevState {
   int32_t arm;           // explore arm chosen for the current level
   int32_t fixed_arm;     // arm used when no scheduler runs (-1 = scheduler)
   uint32_t level_cap;    // levels allowed before BFS_ERR_LEVEL_LIMIT
+  // learned scheduler run inside init and the last block of level
+  // generation (CUDA-graph loop): it stores the next level's explore arm in
+  // `arm`, which explore_any then runs
+  const float *sched_w;      // model weights; null: the scheduler is not fused
+  float sched_min_conf;      // below this top probability: the fallback arm
+  float sched_diam;          // graph-level feature constants
+  float sched_avg_deg_x;
+  unsigned long long sched_cond0; // switch conditions to set with the arm (0: none)
+  unsigned long long sched_cond;
   // per-level record (first BFS_MAX_RECORDED_LEVELS levels)
   uint32_t *rec_frontier;
   uint32_t *rec_edges;
-  int32_t *rec_arm;
+  int32_t *rec_arm;          // arm chosen by a scheduler on the device, -1 if none
+  int32_t *rec_ran;          // arm of the explore kernel that ran
   uint32_t rec_cap;
 };
 

@@ -32,10 +32,9 @@
 #include "engine.h"
 #include "kernels.h"
 #include "bfs_sched.h"
+#include "bfs_sched_dev.cuh"
 
 namespace bfsgb {
-
-constexpr uint32_t kFullMask = 0xFFFFFFFFu;
 
 SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz) {
   SchedGraphConst c;
@@ -46,85 +45,11 @@ SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz) {
   return c;
 }
 
-__device__ __forceinline__ void level_features(const BfsDevState *st, SchedGraphConst gc,
-                                               float x[kSchedIn]) {
-  x[0] = log2f(1.f + (float)st->F) / 32.f;
-  x[1] = log2f(1.f + (float)st->EF) / 32.f;
-  x[2] = 1.f - (float)st->reached / (float)st->n_cols;
-  x[3] = fminf((float)st->lvl / gc.diam, 8.f) / 8.f;
-  x[4] = gc.avg_deg_x;
-}
-
-// Forward pass of one sample by one warp.  Returns this lane's output logit
-// (meaningful on lanes < 9) and the lane's hidden activations.
-__device__ __forceinline__ float mlp_forward(const float *__restrict__ w,
-                                             const float x[kSchedIn], uint32_t lane,
-                                             float *h1_out, float *h2_out) {
-  float a = w[kB1 + lane];
-#pragma unroll
-  for (int i = 0; i < kSchedIn; i++) a = fmaf(w[kW1 + lane * kSchedIn + i], x[i], a);
-  const float h1 = fmaxf(a, 0.f);
-  float b = w[kB2 + lane];
-#pragma unroll 8
-  for (int k = 0; k < kSchedHidden; k++)
-    b = fmaf(w[kW2 + lane * kSchedHidden + k], __shfl_sync(kFullMask, h1, k), b);
-  const float h2 = fmaxf(b, 0.f);
-  const bool out_lane = lane < (uint32_t)kSchedArms;
-  float c = out_lane ? w[kB3 + lane] : 0.f;
-#pragma unroll 8
-  for (int k = 0; k < kSchedHidden; k++) {
-    const float hk = __shfl_sync(kFullMask, h2, k);
-    if (out_lane) c = fmaf(w[kW3 + lane * kSchedHidden + k], hk, c);
-  }
-  *h1_out = h1;
-  *h2_out = h2;
-  return c;
-}
-
-// Softmax over lanes 0..8: returns p on output lanes, 0 elsewhere; *best and
-// *pbest receive the argmax (lowest lane on ties) and its probability.
-__device__ __forceinline__ float softmax9(float z, uint32_t lane, int *best, float *pbest) {
-  const bool out_lane = lane < (uint32_t)kSchedArms;
-  float m = out_lane ? z : -INFINITY;
-  int idx = out_lane ? (int)lane : 1 << 20;
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
-    const float om = __shfl_xor_sync(kFullMask, m, d);
-    const int oi = __shfl_xor_sync(kFullMask, idx, d);
-    if (om > m || (om == m && oi < idx)) {
-      m = om;
-      idx = oi;
-    }
-  }
-  const float e = out_lane ? expf(z - m) : 0.f;
-  float s = e;
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(kFullMask, s, d);
-  *best = idx;
-  *pbest = 1.f / s;  // exp(0) / sum
-  return e / s;
-}
-
 __global__ void sched_kernel(BfsDevState *st, const float *__restrict__ w, float min_conf,
                              SchedGraphConst gc, unsigned long long cond, int use_cond) {
-  const uint32_t lane = threadIdx.x & 31u;
   if (threadIdx.x >= 32) return;
-  int arm = kFallbackArm;
-  if (w != nullptr && st->F > 0) {
-    float x[kSchedIn];
-    level_features(st, gc, x);
-    float h1, h2, pbest;
-    int best;
-    const float z = mlp_forward(w, x, lane, &h1, &h2);
-    softmax9(z, lane, &best, &pbest);
-    arm = (pbest >= min_conf) ? best : kFallbackArm;
-  }
-  if (lane == 0) {
-    st->arm = arm;
-    st->launches += 1;
-    if (st->lvl < st->rec_cap) st->rec_arm[st->lvl] = arm;
-    if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (unsigned)arm);
-  }
+  sched_pick_warp(st, w, min_conf, gc, cond, use_cond != 0);
+  if (threadIdx.x == 0) st->launches += 1;
 }
 
 __global__ void features_kernel(const BfsDevState *st, SchedGraphConst gc, float *out) {

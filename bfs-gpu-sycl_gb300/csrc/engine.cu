@@ -104,7 +104,7 @@ static bfs_status setup_workspace(bfs_graph *g) {
   const size_t nq = std::max<size_t>(g->n_rows, 1);
   const size_t q4 = align_up(nq * 4, 256), qp4 = align_up((nq + 1) * 4, 256);
   const size_t rec = align_up((size_t)BFS_MAX_RECORDED_LEVELS * 4, 256);
-  g->ws_bytes = 2 * bm + 2 * (2 * q4 + qp4) + 3 * rec;
+  g->ws_bytes = 2 * bm + 2 * (2 * q4 + qp4) + 4 * rec;
   CK(cudaMalloc(&g->ws, g->ws_bytes));
   char *p = (char *)g->ws;
   BfsDevState &s = g->tmpl;
@@ -124,6 +124,7 @@ static bfs_status setup_workspace(bfs_graph *g) {
   s.rec_frontier = (uint32_t *)p; p += rec;
   s.rec_edges = (uint32_t *)p; p += rec;
   s.rec_arm = (int32_t *)p; p += rec;
+  s.rec_ran = (int32_t *)p; p += rec;
   s.rec_cap = BFS_MAX_RECORDED_LEVELS;
   s.fixed_arm = 0;
   s.level_cap = g->n_cols + 1u;
@@ -139,6 +140,10 @@ static bfs_status setup_workspace(bfs_graph *g) {
           &occ, explore_kernel_fn(arm, u ? 8 : 4, false), arm_block(arm), 0));
       g->occ[u][arm] = std::max(occ, 1);
     }
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, explore_any_kernel_fn(u ? 8 : 4, false),
+                                                     kAnyBlock, 0));
+    g->occ_any[u] = std::max(occ, 1);
   }
   int occ_lg = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
@@ -261,6 +266,10 @@ static int persistent_blocks(const bfs_graph *g, int arm, int sm_factor, int ipt
   return std::max(1, g->num_sms * per_sm);
 }
 
+static int any_blocks(const bfs_graph *g, int ipt) {
+  return std::max(1, g->num_sms * g->occ_any[ipt == 8 ? 1 : 0]);
+}
+
 // Grid for a host-driven launch with known frontier F (entries) and EF (edges).
 static int host_blocks(const bfs_graph *g, int arm, int sm_factor, int ipt, uint32_t F,
                        uint32_t EF) {
@@ -309,9 +318,11 @@ static cudaError_t add_kernel(cudaGraph_t graph, cudaGraphNode_t *node,
 
 // Builds the device-side level loop:
 //   memset(bitmaps) -> fill(levels/parents) -> init(root) -> while(F > 0) {
-//     explore<arm> -> levelgen (last block sets the while condition) }
-// With arm < 0 (learned schedule) the body is
-//     sched (sets the switch value) -> switch(arm) { 9 explore kernels } -> levelgen
+//     explore -> levelgen (last block sets the while condition) }
+// With a fixed arm the explore node is that arm's kernel.  With arm < 0
+// (learned schedule) it is explore_any, which runs the arm in st->arm: the
+// scheduler runs inside init (level 0) and inside the last block of level
+// generation (the next level), so the loop has no node of its own for it.
 static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt,
                                    GraphEntry *ge) {
   cudaGraph_t graph = nullptr;
@@ -352,32 +363,11 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   if (arm >= 0) {
     CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt, g->run_parents),
                   persistent_blocks(g, arm, sm_factor, ipt), arm_block(arm), ex_args));
-    set_window(g, n_explore);
   } else {
-    cudaGraphConditionalHandle sw;
-    CK(cudaGraphConditionalHandleCreate(&sw, body, 0, cudaGraphCondAssignDefault));
-    unsigned long long sw_arg = (unsigned long long)sw;
-    const float *w = g->sched ? g->sched->d_w : nullptr;
-    float min_conf = g->sched ? g->sched->min_conf : 0.f;
-    SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
-    cudaGraphNode_t n_sched;
-    void *sc_args[] = {&st, &w, &min_conf, &gc, &sw_arg, &one};
-    CK(add_kernel(body, &n_sched, nullptr, 0, sched_kernel_fn(), 1, 32, sc_args));
-    alignas(cudaGraphNodeParams) unsigned char sbuf[sizeof(cudaGraphNodeParams)] = {};
-    cudaGraphNodeParams &sp = *reinterpret_cast<cudaGraphNodeParams *>(sbuf);
-    sp.type = cudaGraphNodeTypeConditional;
-    sp.conditional.handle = sw;
-    sp.conditional.type = cudaGraphCondTypeSwitch;
-    sp.conditional.size = kNumArms;
-    CK(cudaGraphAddNode(&n_explore, body, &n_sched, nullptr, 1, &sp));
-    for (int a = 0; a < kNumArms; a++) {
-      cudaGraphNode_t n_arm;
-      CK(add_kernel(sp.conditional.phGraph_out[a], &n_arm, nullptr, 0,
-                    explore_kernel_fn(a, ipt, g->run_parents),
-                    persistent_blocks(g, a, sm_factor, ipt), arm_block(a), ex_args));
-      set_window(g, n_arm);
-    }
+    CK(add_kernel(body, &n_explore, nullptr, 0, explore_any_kernel_fn(ipt, g->run_parents),
+                  any_blocks(g, ipt), kAnyBlock, ex_args));
   }
+  set_window(g, n_explore);
   void *lg_args[] = {&st, &cond_arg, &one};
   CK(add_kernel(body, &n_lg, &n_explore, 1, levelgen_kernel_fn(), g->lg_grid, kLevelgenBlock,
                 lg_args));
@@ -503,7 +493,10 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     cudaGetLastError();
   }
 
-  const int arm = (o.lb == BFS_LB_LEARNED) ? -1 : arm_of(o.lb, o.block);
+  // learned without a model: the scheduler's fallback arm on every level
+  const bool have_model = g->sched != nullptr && g->sched->d_w != nullptr;
+  const int arm = (o.lb == BFS_LB_LEARNED) ? (have_model ? -1 : kFallbackArm)
+                                           : arm_of(o.lb, o.block);
   g->prof_explore = g->prof_gen = nullptr;
   if (o.record >= 2 && stats) {
     g->prof_explore = stats->level_explore_ms;
@@ -517,18 +510,26 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
   s.level = levels_dev;
   s.parent = parents_dev;
   s.fixed_arm = arm;
-  CK(cudaEventRecord(g->ev0, g->stream));
-  CK(cudaMemcpyAsync(g->d_st, g->h_st, sizeof(BfsDevState), cudaMemcpyHostToDevice, g->stream));
+  const bool graph_loop = o.loop == BFS_LOOP_GRAPH && !timer && o.record < 2;
+  GraphEntry *ge = nullptr;
   bfs_status rc;
-  uint32_t launches = 0;
-  bool host_driven = false;
-  if (o.loop == BFS_LOOP_GRAPH && !timer && o.record < 2) {
-    GraphEntry *ge = nullptr;
+  if (graph_loop) {
     rc = get_loop_graph(g, arm, o.sm_factor, o.ipt, &ge);
     if (rc != BFS_OK) return rc;
+    if (arm < 0) {  // scheduler fused into init and level generation
+      const SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
+      s.sched_w = g->sched->d_w;
+      s.sched_min_conf = g->sched->min_conf;
+      s.sched_diam = gc.diam;
+      s.sched_avg_deg_x = gc.avg_deg_x;
+    }
+  }
+  CK(cudaEventRecord(g->ev0, g->stream));
+  CK(cudaMemcpyAsync(g->d_st, g->h_st, sizeof(BfsDevState), cudaMemcpyHostToDevice, g->stream));
+  uint32_t launches = 0;
+  if (graph_loop) {
     CK(cudaGraphLaunch(ge->exec, g->stream));
   } else {
-    host_driven = true;
     rc = host_loop(g, arm, o.sm_factor, o.ipt, timer);
     if (rc != BFS_OK) return rc;
     launches = g->host_launches;
@@ -559,10 +560,21 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
       CK(cudaMemcpy(stats->level_frontier, g->tmpl.rec_frontier, nrec * 4, cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(stats->level_edges, g->tmpl.rec_edges, nrec * 4, cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(stats->level_arm, g->tmpl.rec_arm, nrec * 4, cudaMemcpyDeviceToHost));
+      std::vector<int32_t> ran(nrec);
+      CK(cudaMemcpy(ran.data(), g->tmpl.rec_ran, nrec * 4, cudaMemcpyDeviceToHost));
+      // level_arm = the explore kernel that ran; where a scheduler chose the
+      // arm on the device, the kernel that ran must be its choice
       for (uint32_t i = 0; i < nrec; i++) {
-        if (stats->level_arm[i] >= 0) continue;
-        if (stats->level_frontier[i] == 0) continue;
-        stats->level_arm[i] = host_driven ? g->host_arms[i] : arm;
+        if (stats->level_frontier[i] == 0) {
+          stats->level_arm[i] = -1;
+          continue;
+        }
+        const int32_t chosen = stats->level_arm[i];
+        if (chosen >= 0 && ran[i] != chosen)
+          return fail(BFS_ERR_DEVICE, "level " + std::to_string(i) + ": explore arm " +
+                                          std::to_string(ran[i]) + " ran, scheduler chose " +
+                                          std::to_string(chosen));
+        stats->level_arm[i] = ran[i];
       }
     }
   }

@@ -64,6 +64,7 @@ struct bfs_graph {
   float *prof_explore = nullptr;  // host arrays filled by the host loop (record == 2)
   float *prof_gen = nullptr;
   int occ[2][bfsgb::kNumArms] = {};  // blocks per SM, [ipt == 8][arm]
+  int occ_any[2] = {};                // blocks per SM of explore_any, [ipt == 8]
   int lg_grid = 0;
   bool l2_pinned = false;
   bool use_l2_pin = true;

@@ -35,6 +35,7 @@
 #include "bfs_internal.h"
 #include "device_util.cuh"
 #include "kernels.h"
+#include "bfs_sched_dev.cuh"
 
 namespace bfsgb {
 
@@ -83,10 +84,36 @@ __global__ void fill_kernel(BfsDevState *st) {
     level[i] = -1;
     if (parent) parent[i] = -1;
   }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < st->rec_cap; i += stride)
+    st->rec_ran[i] = -1;
 }
 
-__global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_cond) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Records, for the level being explored, which explore kernel ran.
+template <int ARM>
+__device__ __forceinline__ void note_arm(BfsDevState *st) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t l = st->lvl;
+    if (l < st->rec_cap) st->rec_ran[l] = ARM;
+  }
+}
+template <int B>
+struct BlockIndex {
+  static constexpr int value = B == 128 ? 0 : B == 256 ? 1 : 2;
+};
+
+// One warp: the learned scheduler's arm for the state's current level, with
+// the model and graph constants held in the state, stored in st->arm for
+// explore_any (and, if sw != 0, set as switch condition sw).  Kept out of line
+// so that the callers' register allocation is not affected.
+__device__ __noinline__ void fused_sched_pick(BfsDevState *st, unsigned long long sw,
+                                              int use_cond) {
+  SchedGraphConst gc;
+  gc.diam = st->sched_diam;
+  gc.avg_deg_x = st->sched_avg_deg_x;
+  sched_pick_warp(st, st->sched_w, st->sched_min_conf, gc, sw, use_cond != 0 && sw != 0);
+}
+
+__device__ void init_state(BfsDevState *st, unsigned long long cond, int use_cond) {
   const uint32_t r = st->root;
   st->vis[r >> 5] |= 1u << (r & 31u);
   st->prev[r >> 5] |= 1u << (r & 31u);
@@ -130,6 +157,15 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
 }
 
+// One warp: thread 0 seeds the root and the first frontier; with a fused
+// scheduler the warp then picks level 0's arm.
+__global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_cond) {
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  if (threadIdx.x == 0) init_state(st, cond, use_cond);
+  __syncwarp();
+  if (st->sched_w != nullptr) fused_sched_pick(st, st->sched_cond0, use_cond);
+}
+
 // ---- explore: LLB / SLB -----------------------------------------------------
 // A tile of B frontier entries per block iteration.  LLB takes entries
 // tile*B .. tile*B+B-1; SLB takes tile, tile+T, tile+2T, ... with T the
@@ -147,17 +183,23 @@ struct MinBlocks {
   static constexpr int value = (U <= 4 ? (CONSTRAINED ? 2048 : 1536) : 1024) / B;
 };
 
-template <int B, bool STRIDED, int U, bool PAR>
-__global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
-    explore_local_kernel(BfsDevState *__restrict__ st) {
-  constexpr int NW = B / 32;
-  __shared__ uint32_t s_off[B + 1];
-  __shared__ uint32_t s_dif[B];  // first edge - tile offset, mod 2^32
-  __shared__ uint32_t s_vid[B];
-  __shared__ uint32_t s_wsum[NW];
+// Barrier over the B threads of one (virtual) block: named barrier `id`.
+template <int B>
+__device__ __forceinline__ void vblock_sync(uint32_t id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(B) : "memory");
+}
 
-  const uint32_t F = st->F;
-  if (F == 0) return;
+// LLB / SLB over one (virtual) block of B threads: thread tid of block vb out
+// of nvb, shared arrays of B (+1) entries, barrier `bar`.  The explore kernels
+// below run it either as a real block (tid = threadIdx.x, barrier 0) or as
+// one of several B-thread slices of a 512-thread block.
+template <int B, bool STRIDED, int U, bool PAR>
+__device__ __forceinline__ void explore_local_body(const BfsDevState *__restrict__ st,
+                                                   uint32_t F, uint32_t tid, uint32_t vb,
+                                                   uint32_t nvb, uint32_t *s_off,
+                                                   uint32_t *s_dif, uint32_t *s_vid,
+                                                   uint32_t *s_wsum, uint32_t bar) {
+  constexpr int NW = B / 32;
   const uint32_t cur_q = st->cur;
   const uint32_t *__restrict__ qb = st->qb[cur_q];
   const uint32_t *__restrict__ qp = st->qp[cur_q];
@@ -165,12 +207,12 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
   int32_t *parent = PAR ? st->parent : nullptr;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lane = tid & 31u, warp = tid >> 5;
   const uint32_t num_tiles = (F + B - 1) / B;
   const uint64_t pol = evict_first_policy();
 
-  for (uint32_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
-    const uint32_t slot = STRIDED ? tile + threadIdx.x * num_tiles : tile * B + threadIdx.x;
+  for (uint32_t tile = vb; tile < num_tiles; tile += nvb) {
+    const uint32_t slot = STRIDED ? tile + tid * num_tiles : tile * B + tid;
     uint32_t beg = 0, deg = 0, vid = 0;
     if (slot < F) {
       beg = qb[slot];
@@ -179,20 +221,20 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
     }
     const uint32_t incl = warp_incl_scan(deg, lane);
     if (lane == 31) s_wsum[warp] = incl;
-    __syncthreads();
+    vblock_sync<B>(bar);
     if (warp == 0) {
       uint32_t w = lane < (uint32_t)NW ? s_wsum[lane] : 0u;
       w = warp_incl_scan(w, lane);
       if (lane < (uint32_t)NW) s_wsum[lane] = w;
     }
-    __syncthreads();
+    vblock_sync<B>(bar);
     const uint32_t total = s_wsum[NW - 1];
     const uint32_t off = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
-    s_off[threadIdx.x] = off;
-    s_dif[threadIdx.x] = beg - off;
-    if (PAR) s_vid[threadIdx.x] = vid;
-    if (threadIdx.x == 0) s_off[B] = total;
-    __syncthreads();
+    s_off[tid] = off;
+    s_dif[tid] = beg - off;
+    if (PAR) s_vid[tid] = vid;
+    if (tid == 0) s_off[B] = total;
+    vblock_sync<B>(bar);
 
     // even split of the tile's edges over the warps, in whole warp rounds
     const uint64_t per_warp = (((uint64_t)total + NW - 1) / NW + 31u) & ~31ull;
@@ -233,8 +275,22 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
           if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
       }
     }
-    __syncthreads();
+    vblock_sync<B>(bar);
   }
+}
+
+template <int B, bool STRIDED, int U, bool PAR>
+__global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
+    explore_local_kernel(BfsDevState *__restrict__ st) {
+  __shared__ uint32_t s_off[B + 1];
+  __shared__ uint32_t s_dif[B];  // first edge - tile offset, mod 2^32
+  __shared__ uint32_t s_vid[B];
+  __shared__ uint32_t s_wsum[B / 32];
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  note_arm<(STRIDED ? 2 : 0) * 3 + BlockIndex<B>::value>(st);
+  explore_local_body<B, STRIDED, U, PAR>(st, F, threadIdx.x, blockIdx.x, gridDim.x, s_off, s_dif,
+                                         s_vid, s_wsum, 0u);
 }
 
 // ---- explore: GLB -----------------------------------------------------------
@@ -246,14 +302,13 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
 // (one probe per lane and round), then walks forward: each round loads the
 // next 32 entry starts and first-edge offsets coalesced, and every lane takes
 // its owner's offsets from those registers with shuffles.
-template <int B, int U, bool PAR>
-__global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
-    explore_global_kernel(BfsDevState *__restrict__ st) {
-  constexpr int NW = B / 32;
+// GLB walk of one warp: global warp index gw out of total_warps.
+template <int U, bool PAR>
+__device__ __forceinline__ void explore_global_body(const BfsDevState *__restrict__ st,
+                                                    uint32_t F, uint32_t gw,
+                                                    uint32_t total_warps) {
   constexpr uint32_t kRound = 32u * U;
   constexpr uint32_t kMinChunk = kRound * kGlbGroups;
-  const uint32_t F = st->F;
-  if (F == 0) return;
   const uint32_t EF = st->EF;
   const uint32_t cur_q = st->cur;
   const uint32_t *__restrict__ qb = st->qb[cur_q];
@@ -262,9 +317,8 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
   int32_t *parent = PAR ? st->parent : nullptr;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
   const uint64_t pol = evict_first_policy();
-  const uint32_t total_warps = gridDim.x * NW;
   // about four chunks per warp (each chunk costs one owner search), whole
   // groups of U rounds, at least kMinChunk edges
   uint64_t ch = ((uint64_t)EF + 4ull * total_warps - 1) / (4ull * total_warps);
@@ -272,7 +326,7 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
   const uint32_t CHUNK = (uint32_t)(ch > kMinChunk ? ch : kMinChunk);
   const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
 
-  for (uint32_t c = blockIdx.x * NW + warp; c < n_chunks; c += total_warps) {
+  for (uint32_t c = gw; c < n_chunks; c += total_warps) {
     const uint32_t w0 = c * CHUNK;  // < EF, no overflow
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     // An entry's edge e lives at inds[e + (qb - qp)]: one difference per
@@ -362,6 +416,72 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
         from[u] = from2[u];
       }
     }
+  }
+}
+
+template <int B, int U, bool PAR>
+__global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
+    explore_global_kernel(BfsDevState *__restrict__ st) {
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  note_arm<1 * 3 + BlockIndex<B>::value>(st);
+  explore_global_body<U, PAR>(st, F, blockIdx.x * (B / 32) + (threadIdx.x >> 5),
+                              gridDim.x * (B / 32));
+}
+
+// ---- explore: any arm, chosen on the device ---------------------------------
+// One 512-thread kernel for the learned schedule in the CUDA-graph loop: it
+// runs the arm the scheduler stored in st->arm (init or the last block of the
+// previous level generation picked it), so the loop needs no switch node.
+// GLB does not depend on the block size (edges are dealt per warp over the
+// grid); LLB / SLB tiles of 128 or 256 entries run on 4 or 2 slices of the
+// block, each with its own shared arrays and named barrier.
+template <int U, bool PAR>
+__global__ void __launch_bounds__(kAnyBlock, (U <= 4 ? 2048 : 1024) / kAnyBlock)
+    explore_any_kernel(BfsDevState *__restrict__ st) {
+  __shared__ uint32_t s_off[kAnyBlock + 4];
+  __shared__ uint32_t s_dif[kAnyBlock];
+  __shared__ uint32_t s_vid[kAnyBlock];
+  __shared__ uint32_t s_wsum[kAnyBlock / 32];
+  const uint32_t F = st->F;
+  if (F == 0) return;
+  const int arm = st->arm;  // uniform over the grid
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t l = st->lvl;
+    if (l < st->rec_cap) st->rec_ran[l] = arm;
+  }
+  const int form = arm / 3, bi = arm % 3;
+  const uint32_t t = threadIdx.x;
+  if (form == BFS_LB_GLB) {
+    explore_global_body<U, PAR>(st, F, blockIdx.x * (kAnyBlock / 32) + (t >> 5),
+                                gridDim.x * (kAnyBlock / 32));
+  } else if (bi == 2) {
+    if (form == BFS_LB_SLB)
+      explore_local_body<512, true, U, PAR>(st, F, t, blockIdx.x, gridDim.x, s_off, s_dif, s_vid,
+                                            s_wsum, 1u);
+    else
+      explore_local_body<512, false, U, PAR>(st, F, t, blockIdx.x, gridDim.x, s_off, s_dif,
+                                             s_vid, s_wsum, 1u);
+  } else if (bi == 1) {
+    const uint32_t v = t >> 8, o = v * 257u;
+    if (form == BFS_LB_SLB)
+      explore_local_body<256, true, U, PAR>(st, F, t & 255u, blockIdx.x * 2 + v, gridDim.x * 2,
+                                            s_off + o, s_dif + v * 256, s_vid + v * 256,
+                                            s_wsum + v * 8, 1u + v);
+    else
+      explore_local_body<256, false, U, PAR>(st, F, t & 255u, blockIdx.x * 2 + v, gridDim.x * 2,
+                                             s_off + o, s_dif + v * 256, s_vid + v * 256,
+                                             s_wsum + v * 8, 1u + v);
+  } else {
+    const uint32_t v = t >> 7, o = v * 129u;
+    if (form == BFS_LB_SLB)
+      explore_local_body<128, true, U, PAR>(st, F, t & 127u, blockIdx.x * 4 + v, gridDim.x * 4,
+                                            s_off + o, s_dif + v * 128, s_vid + v * 128,
+                                            s_wsum + v * 4, 1u + v);
+    else
+      explore_local_body<128, false, U, PAR>(st, F, t & 127u, blockIdx.x * 4 + v, gridDim.x * 4,
+                                             s_off + o, s_dif + v * 128, s_vid + v * 128,
+                                             s_wsum + v * 4, 1u + v);
   }
 }
 
@@ -551,9 +671,15 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     s_last = (ticket == gridDim.x - 1);
   }
   __syncthreads();
-  if (s_last && threadIdx.x == 0) {
-    __threadfence();
-    finish_level(st, cond, use_cond);
+  if (s_last && warp == 0) {
+    if (lane == 0) {
+      __threadfence();
+      finish_level(st, cond, use_cond);
+    }
+    __syncwarp();
+    // fused scheduler: the arm of the level just generated, for the
+    // explore_any launch of the next loop iteration
+    if (st->sched_w != nullptr) fused_sched_pick(st, st->sched_cond, use_cond);
   }
 }
 
@@ -663,6 +789,11 @@ static const void *explore_fn_u(int arm) {
 const void *explore_kernel_fn(int arm, int ipt, bool parents) {
   if (parents) return ipt == 8 ? explore_fn_u<8, true>(arm) : explore_fn_u<4, true>(arm);
   return ipt == 8 ? explore_fn_u<8, false>(arm) : explore_fn_u<4, false>(arm);
+}
+const void *explore_any_kernel_fn(int ipt, bool parents) {
+  if (parents)
+    return ipt == 8 ? (const void *)explore_any_kernel<8, true> : (const void *)explore_any_kernel<4, true>;
+  return ipt == 8 ? (const void *)explore_any_kernel<8, false> : (const void *)explore_any_kernel<4, false>;
 }
 const void *levelgen_kernel_fn() { return (const void *)levelgen_kernel<kLevelgenBlock>; }
 const void *init_kernel_fn() { return (const void *)init_kernel; }

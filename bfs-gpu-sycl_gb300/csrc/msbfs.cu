@@ -6,20 +6,27 @@
 // reached by root j) and the frontier queue carries, per entry, the mask of
 // roots whose frontier contains it.  One traversal of an edge u->v serves every
 // root whose frontier holds u:  next[v] |= mask(u) & ~visited[v].
-// Level generation turns next[] into the new frontier, writes each root's
-// int32 level row and each root's edgesCount (sum of degrees of the vertices
-// that root expands, run_bfs_cpu.hpp:36), so every row is exactly the
-// single-root level array of its root.
+// Level generation turns next[] into the new frontier and records, per
+// level, the mask of roots that reached each vertex; an expansion kernel
+// writes each root's int32 level row once, coalesced, from those masks, and
+// each root's edgesCount (sum of degrees of the vertices that root expands,
+// run_bfs_cpu.hpp:36), so every row is exactly the single-root level array
+// of its root.
 //
 //   explore   edge-balanced like the GLB form: a warp takes a chunk of the
 //             frontier's edges, finds the owner of its first edge with a 32-ary
 //             search of the degree prefix, then takes each owner's first edge
 //             and root mask from shuffles of coalesced loads.
-//   levelgen  one vertex per lane: new = next[v] & ~visited[v]; the warp
-//             iterates over the union of new bits, storing level[j][v] for the
-//             lanes holding bit j (coalesced per root row) and reducing those
-//             lanes' degrees into root j's edge counter; kept vertices are
-//             compacted with ballot/popc and one atomic per block.
+//   levelgen  one vertex per lane: new = next[v] & ~visited[v], stored as
+//             hist[L][v] for the first kHistLevels levels (one coalesced 8-byte
+//             store per vertex; level rows written level by level would be
+//             scattered partial-sector stores, which HBM turns into
+//             read-modify-writes); kept vertices are compacted with
+//             ballot/popc and one atomic per block.
+//   expand    one warp per 32 vertices writes every root's 32 level entries
+//             as one 128-byte segment (-1 where unreached), once per pass; if
+//             the search goes past the history it runs at that point and the
+//             deeper levels are stored into the rows directly.
 //   loop      a CUDA graph with a conditional WHILE node, as for one root.
 #include <cuda_runtime.h>
 
@@ -39,6 +46,8 @@ constexpr int kLanes = 64;
 constexpr int kMsBlock = 256;
 constexpr int kMsU = 4;
 constexpr uint32_t kMsChunk = 32u * kMsU * 4u;
+// Levels kept as per-vertex root masks before the rows are written.
+constexpr uint32_t kHistLevels = 16;
 
 struct MsState {
   const uint32_t *indptr;
@@ -46,6 +55,7 @@ struct MsState {
   uint32_t n_rows, n_cols;
   unsigned long long *vis;
   unsigned long long *next;
+  unsigned long long *hist;  // kHistLevels arrays of n_cols masks
   uint32_t *qb[2];
   uint32_t *qp[2];
   unsigned long long *qm[2];
@@ -59,33 +69,16 @@ struct MsState {
   unsigned long long edges[kLanes];
 };
 
-__global__ void ms_fill_kernel(MsState *st) {
-  int32_t *level = st->level;
-  const uint64_t total = (uint64_t)st->n_lanes * st->n_cols;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const bool vec = (reinterpret_cast<uintptr_t>(level) & 15u) == 0;
-  const uint64_t n4 = vec ? total / 4 : 0;
-  const int4 neg = make_int4(-1, -1, -1, -1);
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
-    reinterpret_cast<int4 *>(level)[i] = neg;
-  for (uint64_t i = n4 * 4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += stride)
-    level[i] = -1;
-}
-
 // One block of 64 threads: seeds every root and builds the first frontier
 // (roots shared by several lanes become one entry with several mask bits).
 __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_cond) {
   const uint32_t j = threadIdx.x;
-  const uint32_t n = st->n_cols;
   if (j < st->n_lanes) {
     const uint32_t r = st->roots[j];
-    st->level[(size_t)j * n + r] = 0;
     atomicOr(&st->vis[r], 1ull << j);
-    st->edges[j] = r < st->n_rows ? (unsigned long long)(st->indptr[r + 1] - st->indptr[r]) : 0ull;
-  } else if (j < kLanes) {
-    st->edges[j] = 0;
+    atomicOr(&st->hist[r], 1ull << j);  // level 0
   }
+  if (j < kLanes) st->edges[j] = 0;
   __syncthreads();
   if (j == 0) {
     uint32_t F = 0, EF = 0;
@@ -116,15 +109,19 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
     st->error = 0;
     st->max_level = 0;
     st->any_new = 0;
-    st->launches = 3;
+    st->launches = 2;  // memset, init
     if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, F > 0);
   }
 }
 
+// Explore: the single-root GLB walk (one difference per entry, a 32-entry
+// window re-based only when a round could leave it) with a root mask per
+// entry: next[v] |= mask(u) & ~vis[v].
 __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     ms_explore_kernel(MsState *__restrict__ st) {
   constexpr int NW = kMsBlock / 32;
-  constexpr uint32_t kRound = 32u * kMsU;
+  constexpr int U = kMsU;
+  constexpr uint32_t kRound = 32u * U;
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t EF = st->EF;
@@ -148,50 +145,52 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     const uint32_t w0 = c * CHUNK;
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
-    uint32_t cur_start = qp[cur], cur_beg = qb[cur];
+    uint32_t cur_d = qb[cur] - qp[cur];
     unsigned long long cur_mask = qm[cur];
-    uint32_t j = cur + 1u + lane;
-    uint32_t bnd = (j <= F) ? qp[j] : kFull;
-    uint32_t bg = (j < F) ? qb[j] : 0u;
-    unsigned long long mk = (j < F) ? qm[j] : 0ull;
+    uint32_t c0 = cur;
+    uint32_t bnd = (c0 + 1u + lane <= F) ? qp[c0 + 1u + lane] : kFull;
+    uint32_t dl = (c0 + 1u + lane < F) ? qb[c0 + 1u + lane] - bnd : 0u;
+    unsigned long long mk = (c0 + 1u + lane < F) ? qm[c0 + 1u + lane] : 0ull;
+    uint32_t wlast = __shfl_sync(kFull, bnd, 31);
     for (uint32_t base = w0; base < w1; base += kRound) {
-      uint32_t addr[kMsU];
-      unsigned long long msk[kMsU];
+      uint32_t ad[U], nb[U];
+      unsigned long long msk[U];
 #pragma unroll
-      for (int u = 0; u < kMsU; u++) {
+      for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
         const uint32_t e = rb + lane;
+        if (wlast < rb || wlast - rb < 31u) {  // warp-uniform
+          c0 = cur;
+          const uint32_t j = c0 + 1u + lane;
+          bnd = (j <= F) ? qp[j] : kFull;
+          dl = (j < F) ? qb[j] - bnd : 0u;
+          mk = (j < F) ? qm[j] : 0ull;
+          wlast = __shfl_sync(kFull, bnd, 31);
+        }
         const uint32_t p = bnd - rb;
         const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
         const uint32_t k = __popc(starts & ((2u << lane) - 1u));
-        const uint32_t srcl = k ? k - 1u : 0u;
-        const uint32_t s_start = __shfl_sync(kFull, bnd, srcl);
-        const uint32_t s_beg = __shfl_sync(kFull, bg, srcl);
+        const uint32_t srcl = k ? cur + k - c0 - 1u : 0u;
+        const uint32_t s_d = __shfl_sync(kFull, dl, srcl);
         const unsigned long long s_mask = __shfl_sync(kFull, mk, srcl);
-        addr[u] = kFull;
+        ad[u] = kFull;
         msk[u] = 0;
         if (e < w1) {
-          addr[u] = (k ? s_beg : cur_beg) + (e - (k ? s_start : cur_start));
+          ad[u] = e + (k ? s_d : cur_d);
           msk[u] = k ? s_mask : cur_mask;
         }
-        const uint32_t k31 = __shfl_sync(kFull, k, 31);
+        const uint32_t k31 = __popc(starts);
         if (k31) {
           cur += k31;
-          cur_start = __shfl_sync(kFull, bnd, k31 - 1u);
-          cur_beg = __shfl_sync(kFull, bg, k31 - 1u);
-          cur_mask = __shfl_sync(kFull, mk, k31 - 1u);
-          j = cur + 1u + lane;
-          bnd = (j <= F) ? qp[j] : kFull;
-          bg = (j < F) ? qb[j] : 0u;
-          mk = (j < F) ? qm[j] : 0ull;
+          cur_d = __shfl_sync(kFull, dl, cur - c0 - 1u);
+          cur_mask = __shfl_sync(kFull, mk, cur - c0 - 1u);
         }
       }
-      uint32_t nb[kMsU];
 #pragma unroll
-      for (int u = 0; u < kMsU; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
+      for (int u = 0; u < U; u++) nb[u] = ad[u] != kFull ? ld_stream(inds + ad[u], pol) : kFull;
 #pragma unroll
-      for (int u = 0; u < kMsU; u++) {
-        if (addr[u] == kFull) continue;
+      for (int u = 0; u < U; u++) {
+        if (nb[u] == kFull) continue;
         const unsigned long long bits = msk[u] & ~vis[nb[u]];
         if (bits) atomicOr(next + nb[u], bits);
       }
@@ -213,7 +212,7 @@ __device__ void ms_finish(MsState *st, unsigned long long cond, int use_cond) {
   st->lvl = lvl;
   st->next_packed = 0;
   st->done_blocks = 0;
-  st->launches += 2;
+  st->launches += 3;  // explore, levelgen, expand check
   if (f_new > 0 && lvl >= st->level_cap) {
     st->error |= BFS_DEVERR_LEVEL_LIMIT;
     st->F = 0;
@@ -221,11 +220,15 @@ __device__ void ms_finish(MsState *st, unsigned long long cond, int use_cond) {
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
 }
 
+// Level generation, one vertex per thread: new = next[v] & ~vis[v].  Levels
+// below kHistLevels are recorded as masks, hist[L][v] = new (written for
+// every vertex, coalesced; ms_expand_kernel turns them into the level rows);
+// deeper levels are written straight into the rows.  Kept vertices are
+// compacted with ballot/popc and one atomic per block.
 __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restrict__ st,
                                                                unsigned long long cond,
                                                                int use_cond) {
   constexpr int NW = kMsBlock / 32;
-  __shared__ unsigned long long s_edges[kLanes];
   __shared__ unsigned long long s_wtot[NW];
   __shared__ unsigned long long s_base;
   __shared__ int s_last;
@@ -235,14 +238,15 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
   unsigned long long *__restrict__ next = st->next;
   const uint32_t *__restrict__ indptr = st->indptr;
   int32_t *__restrict__ level = st->level;
-  const int32_t lvl_next = (int32_t)st->lvl + 1;
+  const uint32_t L = st->lvl + 1;
+  unsigned long long *__restrict__ hist =
+      L < kHistLevels ? st->hist + (size_t)L * n_cols : nullptr;
   const uint32_t nq = st->cur ^ 1u;
   uint32_t *__restrict__ qb = st->qb[nq];
   uint32_t *__restrict__ qp = st->qp[nq];
   unsigned long long *__restrict__ qm = st->qm[nq];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  if (threadIdx.x < kLanes) s_edges[threadIdx.x] = 0;
   if (threadIdx.x == 0) s_any = 0;
   __syncthreads();
   bool any = false;
@@ -265,26 +269,22 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
           }
         }
       }
+      if (hist) hist[v] = nw;
     }
     any |= nw != 0;
+    if (!hist) {  // past the history: one root row at a time
+      const uint32_t u_lo = __reduce_or_sync(kFull, (uint32_t)nw);
+      const uint32_t u_hi = __reduce_or_sync(kFull, (uint32_t)(nw >> 32));
+      for (uint32_t m = u_lo; m; m &= m - 1u) {
+        const uint32_t j = __ffs(m) - 1u;
+        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + v] = (int32_t)L;
+      }
+      for (uint32_t m = u_hi; m; m &= m - 1u) {
+        const uint32_t j = 32u + __ffs(m) - 1u;
+        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + v] = (int32_t)L;
+      }
+    }
     const uint32_t deg = e - b;
-    // levels and per-root edge counts, one root row at a time
-    const uint32_t u_lo = __reduce_or_sync(kFull, (uint32_t)nw);
-    const uint32_t u_hi = __reduce_or_sync(kFull, (uint32_t)(nw >> 32));
-    for (uint32_t m = u_lo; m; m &= m - 1u) {
-      const uint32_t j = __ffs(m) - 1u;
-      const bool has = (nw >> j) & 1ull;
-      if (has) level[(size_t)j * n_cols + v] = lvl_next;
-      const uint32_t ds = __reduce_add_sync(kFull, has ? deg : 0u);
-      if (lane == 0 && ds) atomicAdd(&s_edges[j], (unsigned long long)ds);
-    }
-    for (uint32_t m = u_hi; m; m &= m - 1u) {
-      const uint32_t j = 32u + __ffs(m) - 1u;
-      const bool has = (nw >> j) & 1ull;
-      if (has) level[(size_t)j * n_cols + v] = lvl_next;
-      const uint32_t ds = __reduce_add_sync(kFull, has ? deg : 0u);
-      if (lane == 0 && ds) atomicAdd(&s_edges[j], (unsigned long long)ds);
-    }
     // compact the kept vertices: ballot/popc per warp, one atomic per block
     const uint32_t km = __ballot_sync(kFull, deg > 0u);
     const uint32_t dincl = warp_incl_scan(deg, lane);
@@ -311,8 +311,6 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
   }
   if (any) s_any = 1;
   __syncthreads();
-  if (threadIdx.x < kLanes && s_edges[threadIdx.x])
-    atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x]);
   if (threadIdx.x == 0) {
     if (s_any) atomicOr(&st->any_new, 1u);
     __threadfence();
@@ -323,6 +321,102 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
   if (s_last && threadIdx.x == 0) {
     __threadfence();
     ms_finish(st, cond, use_cond);
+  }
+}
+
+// Writes the level rows from the history and, after the last level, the
+// per-root edge counts.  In the level loop (final == 0) it acts only once,
+// right after the last history level when the search goes on: it then
+// writes every row entry (level or -1) so that level generation can write
+// the deeper levels directly.  After the loop (final != 0) it writes the rows
+// unless that already happened (the search went past the history), then
+// adds, per root, the degrees of the vertices < n_rows it reached
+// (run_bfs_cpu.hpp:36).
+//
+// One warp per 32 consecutive vertices, lane = vertex.  History levels are
+// < 16, so a lane ORs its vertex's masks into four bit planes (plane k holds
+// the roots whose level has bit k set) and a reached mask; the level of root
+// j is then four bit extracts, and the warp stores root j's 32 entries as one
+// 128-byte segment.  The root loop is unrolled so that every shift is a
+// constant.
+template <int H>
+__device__ __forceinline__ void ms_store_rows(int32_t *__restrict__ row, size_t n, uint32_t v,
+                                              bool in, uint32_t nl, uint32_t r, uint32_t b0,
+                                              uint32_t b1, uint32_t b2, uint32_t b3) {
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    if ((uint32_t)(H * 32 + j) >= nl) break;  // uniform
+    const int32_t x = (int32_t)(((b0 >> j) & 1u) | (((b1 >> j) & 1u) << 1) |
+                                (((b2 >> j) & 1u) << 2) | (((b3 >> j) & 1u) << 3));
+    if (in) row[v] = ((r >> j) & 1u) ? x : -1;
+    row += n;
+  }
+}
+
+__global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restrict__ st,
+                                                                int final) {
+  static_assert(kHistLevels <= 16, "levels must fit four bit planes");
+  __shared__ unsigned long long s_edges[kLanes];
+  const uint32_t lvl = st->lvl;
+  const bool expand = final ? (lvl < kHistLevels) : (lvl + 1u == kHistLevels && st->F > 0);
+  if (!final && !expand) return;  // uniform over the grid
+  const uint32_t n = st->n_cols, n_rows = st->n_rows, nl = st->n_lanes;
+  const uint32_t lmax = lvl < kHistLevels ? lvl : kHistLevels - 1u;
+  const unsigned long long *__restrict__ hist = st->hist;
+  const unsigned long long *__restrict__ vis = st->vis;
+  const uint32_t *__restrict__ indptr = st->indptr;
+  int32_t *__restrict__ level = st->level;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (final) {
+    if (threadIdx.x < kLanes) s_edges[threadIdx.x] = 0;
+    __syncthreads();
+  }
+  const uint64_t stride = (uint64_t)gridDim.x * kMsBlock;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * kMsBlock + warp * 32u; t0 < n; t0 += stride) {
+    const uint32_t v = (uint32_t)t0 + lane;
+    const bool in = v < n;
+    if (expand) {
+      unsigned long long r = 0, p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+      if (in) {
+        for (uint32_t L = 0; L <= lmax; L++) {
+          const unsigned long long m = hist[(size_t)L * n + v];
+          r |= m;
+          if (L & 1u) p0 |= m;
+          if (L & 2u) p1 |= m;
+          if (L & 4u) p2 |= m;
+          if (L & 8u) p3 |= m;
+        }
+      }
+      ms_store_rows<0>(level, n, v, in, nl, (uint32_t)r, (uint32_t)p0, (uint32_t)p1,
+                       (uint32_t)p2, (uint32_t)p3);
+      if (nl > 32)
+        ms_store_rows<1>(level + (size_t)32 * n, n, v, in, nl, (uint32_t)(r >> 32),
+                         (uint32_t)(p0 >> 32), (uint32_t)(p1 >> 32), (uint32_t)(p2 >> 32),
+                         (uint32_t)(p3 >> 32));
+    }
+    if (final) {
+      const unsigned long long vm = in ? vis[v] : 0ull;
+      const uint32_t deg = (in && v < n_rows && vm) ? indptr[v + 1] - indptr[v] : 0u;
+      if (__ballot_sync(kFull, deg > 0u)) {
+        // 32 degrees of distinct vertices sum to at most nnz < 2^32
+        const uint32_t lo = (uint32_t)vm, hi = (uint32_t)(vm >> 32);
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const uint32_t a = __reduce_add_sync(kFull, ((lo >> j) & 1u) ? deg : 0u);
+          const uint32_t c = __reduce_add_sync(kFull, ((hi >> j) & 1u) ? deg : 0u);
+          if (lane == 0) {
+            if (a) atomicAdd(&s_edges[j], (unsigned long long)a);
+            if (c) atomicAdd(&s_edges[32 + j], (unsigned long long)c);
+          }
+        }
+      }
+    }
+  }
+  if (final) {
+    __syncthreads();
+    if (threadIdx.x < nl && s_edges[threadIdx.x])
+      atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->launches += 1;
   }
 }
 
@@ -339,8 +433,8 @@ struct MsWorkspace {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  int grid_ex = 0, grid_lg = 0, grid_fill = 0;
-  size_t clear_bytes = 0;  // visited + next masks, cleared before each pass
+  int grid_ex = 0, grid_lg = 0, grid_xp = 0;
+  size_t clear_bytes = 0;  // visited and next masks, history level 0
 };
 
 namespace bfsgb {
@@ -376,7 +470,7 @@ static bfs_status ms_setup(bfs_graph *g) {
   const size_t n = g->n_cols, nr = std::max<uint32_t>(g->n_rows, 1);
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t b64 = al(n * 8), q4 = al(nr * 4), qp4 = al((nr + 1) * 4), q8 = al(nr * 8);
-  const size_t bytes = 2 * b64 + 2 * (q4 + qp4 + q8);
+  const size_t bytes = (2 + kHistLevels) * b64 + 2 * (q4 + qp4 + q8);
   MK(cudaMalloc(&w->mem, bytes));
   MK(cudaMalloc(&w->d_st, sizeof(MsState)));
   MK(cudaMallocHost(&w->h_st, sizeof(MsState)));
@@ -391,23 +485,27 @@ static bfs_status ms_setup(bfs_graph *g) {
   s.n_cols = g->n_cols;
   s.vis = (unsigned long long *)p; p += b64;
   s.next = (unsigned long long *)p; p += b64;
+  s.hist = (unsigned long long *)p; p += kHistLevels * b64;
   for (int b = 0; b < 2; b++) {
     s.qb[b] = (uint32_t *)p; p += q4;
     s.qp[b] = (uint32_t *)p; p += qp4;
     s.qm[b] = (unsigned long long *)p; p += q8;
   }
   s.level_cap = g->n_cols + 1u;
-  w->clear_bytes = 2 * b64;
-  int occ_ex = 0, occ_lg = 0;
+  w->clear_bytes = 3 * b64;  // vis, next, hist[0] are contiguous
+  int occ_ex = 0, occ_lg = 0, occ_xp = 0;
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, (const void *)ms_explore_kernel,
                                                    kMsBlock, 0));
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, (const void *)ms_levelgen_kernel,
                                                    kMsBlock, 0));
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_xp, (const void *)ms_expand_kernel,
+                                                   kMsBlock, 0));
   w->grid_ex = g->num_sms * std::max(occ_ex, 1);
   w->grid_lg = g->num_sms * std::max(occ_lg, 1);
-  w->grid_fill = g->num_sms * 8;
+  w->grid_xp = g->num_sms * std::max(occ_xp, 1);
 
-  // graph: memset(vis, next) -> fill -> init -> while(F > 0) { explore -> levelgen }
+  // graph: memset(vis, next, hist[0]) -> init ->
+  //   while(F > 0) { explore -> levelgen -> expand(in loop) } -> expand(final)
   MK(cudaGraphCreate(&w->graph, 0));
   cudaGraphConditionalHandle cond;
   MK(cudaGraphConditionalHandleCreate(&cond, w->graph, 0, cudaGraphCondAssignDefault));
@@ -418,24 +516,18 @@ static bfs_status ms_setup(bfs_graph *g) {
   std::memset(&mp, 0, sizeof(mp));
   mp.dst = w->mem;
   mp.elementSize = 4;
-  mp.width = 2 * b64 / 4;
+  mp.width = w->clear_bytes / 4;
   mp.height = 1;
-  cudaGraphNode_t n_ms, n_fill, n_init, n_while, n_ex, n_lg;
+  cudaGraphNode_t n_ms, n_init, n_while, n_ex, n_lg, n_xp, n_xf;
   MK(cudaGraphAddMemsetNode(&n_ms, w->graph, nullptr, 0, &mp));
   cudaKernelNodeParams kp;
   std::memset(&kp, 0, sizeof(kp));
-  void *fill_args[] = {&st};
-  kp.func = (void *)ms_fill_kernel;
-  kp.gridDim = dim3(w->grid_fill);
-  kp.blockDim = dim3(256);
-  kp.kernelParams = fill_args;
-  MK(cudaGraphAddKernelNode(&n_fill, w->graph, &n_ms, 1, &kp));
   void *init_args[] = {&st, &cond_arg, &one};
   kp.func = (void *)ms_init_kernel;
   kp.gridDim = dim3(1);
   kp.blockDim = dim3(kLanes);
   kp.kernelParams = init_args;
-  MK(cudaGraphAddKernelNode(&n_init, w->graph, &n_fill, 1, &kp));
+  MK(cudaGraphAddKernelNode(&n_init, w->graph, &n_ms, 1, &kp));
   alignas(cudaGraphNodeParams) unsigned char wbuf[sizeof(cudaGraphNodeParams)] = {};
   cudaGraphNodeParams &wp = *reinterpret_cast<cudaGraphNodeParams *>(wbuf);
   wp.type = cudaGraphNodeTypeConditional;
@@ -456,6 +548,15 @@ static bfs_status ms_setup(bfs_graph *g) {
   kp.blockDim = dim3(kMsBlock);
   kp.kernelParams = lg_args;
   MK(cudaGraphAddKernelNode(&n_lg, body, &n_ex, 1, &kp));
+  int in_loop = 0, after = 1;
+  void *xp_args[] = {&st, &in_loop};
+  kp.func = (void *)ms_expand_kernel;
+  kp.gridDim = dim3(w->grid_xp);
+  kp.kernelParams = xp_args;
+  MK(cudaGraphAddKernelNode(&n_xp, body, &n_lg, 1, &kp));
+  void *xf_args[] = {&st, &after};
+  kp.kernelParams = xf_args;
+  MK(cudaGraphAddKernelNode(&n_xf, w->graph, &n_while, 1, &kp));
   MK(cudaGraphInstantiate(&w->exec, w->graph, 0));
   return BFS_OK;
 }
@@ -469,8 +570,6 @@ static bfs_status ms_pass_host(bfs_graph *g, MsWorkspace *w) {
   unsigned long long no_cond = 0;
   int zero = 0;
   MK(cudaMemsetAsync(w->mem, 0, w->clear_bytes, s));
-  ms_fill_kernel<<<w->grid_fill, 256, 0, s>>>(st);
-  MK(cudaGetLastError());
   ms_init_kernel<<<1, kLanes, 0, s>>>(st, no_cond, zero);
   MK(cudaGetLastError());
   uint32_t *h_F = &w->h_st->F;
@@ -482,7 +581,11 @@ static bfs_status ms_pass_host(bfs_graph *g, MsWorkspace *w) {
     MK(cudaGetLastError());
     ms_levelgen_kernel<<<w->grid_lg, kMsBlock, 0, s>>>(st, no_cond, zero);
     MK(cudaGetLastError());
+    ms_expand_kernel<<<w->grid_xp, kMsBlock, 0, s>>>(st, 0);
+    MK(cudaGetLastError());
   }
+  ms_expand_kernel<<<w->grid_xp, kMsBlock, 0, s>>>(st, 1);
+  MK(cudaGetLastError());
   return BFS_OK;
 }
 

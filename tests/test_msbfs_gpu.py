@@ -82,3 +82,28 @@ def test_config5a_rmat22_1024_roots(B, O):
         assert np.array_equal(out.cpu().numpy(), ref), b
         assert np.array_equal(ec, rec), b
     dg.free()
+
+
+def test_history_boundary_depths(B, O):
+    """Paths whose searches end just before, at and after the 16-level mask
+    history (the level rows are then written from the history, at the
+    boundary, or partly direct), with the graph and the host loop."""
+    torch = torch_cuda()
+    for n in range(14, 21):
+        src = np.arange(n - 1)
+        u = np.concatenate([src, src + 1])
+        v = np.concatenate([src + 1, src])
+        order = np.lexsort((v, u))
+        indptr = np.zeros(n + 1, np.uint32)
+        np.add.at(indptr, u + 1, 1)
+        g = B.Csc(np.cumsum(indptr).astype(np.uint32), v[order].astype(np.uint32))
+        dg = B.Graph.upload(g)
+        roots = [0, n - 1, n // 2, 1, 0]
+        ref, rec = O.oracle_bfs_many(g.indptr, g.inds, roots)
+        for loop in ("graph", "host"):
+            out = torch.full((len(roots), n), 9, dtype=torch.int32, device="cuda")
+            ec, st = dg.run_batch(roots, out.data_ptr(), loop=loop)
+            assert np.array_equal(out.cpu().numpy(), ref), (n, loop)
+            assert np.array_equal(ec, rec), (n, loop)
+            assert st.max_levels == int(ref.max()) + 1
+        dg.free()

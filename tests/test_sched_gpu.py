@@ -136,3 +136,32 @@ def test_device_choice_equals_batch_prediction(B):
     used = [a for a, fr in zip(tab["arm"], tab["frontier"]) if fr]
     assert used == pred.tolist()
     dg.free()
+
+
+def test_graph_loop_runs_every_arm_exactly(B, O):
+    """A model whose output bias forces one arm runs that arm on every level
+    of the CUDA-graph loop (the one kernel that serves any arm), with and
+    without parents; levels, edge counts and parents are exact."""
+    torch_cuda()
+    graphs = [B.gen_rmat(15, 16, seed=21), B.gen_grid(96, 64, 0.05, 22)]
+    b3 = B.SCHED_PARAMS - B.SCHED_ARMS  # output bias offset (last 9 parameters)
+    for g in graphs:
+        dg = B.Graph.upload(g)
+        roots = B.sample_roots(g, 2, 23)
+        refs = [O.oracle_bfs(g.indptr, g.inds, int(r)) for r in roots]
+        for arm in range(B.SCHED_ARMS):
+            w = np.zeros(B.SCHED_PARAMS, np.float32)
+            w[b3 + arm] = 10.0
+            dg.sched_attach(w)
+            for r, (ref, ec) in zip(roots, refs):
+                lv, pa, st = dg.run(int(r), B.options("learned", record=1), parents=True)
+                assert np.array_equal(lv, ref) and st.edges_count == ec, (arm, int(r))
+                tab = st.levels_table()
+                assert set(a for a, f in zip(tab["arm"], tab["frontier"]) if f) == {arm}
+                reached = lv >= 0
+                assert pa[int(r)] == int(r)
+                kids = np.flatnonzero(reached & (lv > 0))
+                assert np.all(lv[pa[kids]] == lv[kids] - 1)
+                lv2, _, _ = dg.run(int(r), B.options("learned"))
+                assert np.array_equal(lv2, ref)
+        dg.free()

@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
     if (threadIdx.x < kLanes) s_edges[threadIdx.x] = 0;
     __syncthreads();
   }
+  unsigned long long acc_lo = 0, acc_hi = 0;  // degree sums of roots lane, 32 + lane
   const uint64_t stride = (uint64_t)gridDim.x * kMsBlock;
   for (uint64_t t0 = (uint64_t)blockIdx.x * kMsBlock + warp * 32u; t0 < n; t0 += stride) {
     const uint32_t v = (uint32_t)t0 + lane;
@@ -381,10 +382,10 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
         for (uint32_t L = 0; L <= lmax; L++) {
           const unsigned long long m = hist[(size_t)L * n + v];
           r |= m;
-          if (L & 1u) p0 |= m;
-          if (L & 2u) p1 |= m;
-          if (L & 4u) p2 |= m;
-          if (L & 8u) p3 |= m;
+          p0 |= m & (0ull - (L & 1u));
+          p1 |= m & (0ull - ((L >> 1) & 1u));
+          p2 |= m & (0ull - ((L >> 2) & 1u));
+          p3 |= m & (0ull - ((L >> 3) & 1u));
         }
       }
       ms_store_rows<0>(level, n, v, in, nl, (uint32_t)r, (uint32_t)p0, (uint32_t)p1,
@@ -395,24 +396,36 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
                          (uint32_t)(p3 >> 32));
     }
     if (final) {
+      // per-root degree sums as a bit-matrix product: lane j takes the
+      // vertex masks of roots j and 32 + j (32 ballots), and the degrees go
+      // in bit planes (one ballot per degree bit)
       const unsigned long long vm = in ? vis[v] : 0ull;
       const uint32_t deg = (in && v < n_rows && vm) ? indptr[v + 1] - indptr[v] : 0u;
-      if (__ballot_sync(kFull, deg > 0u)) {
-        // 32 degrees of distinct vertices sum to at most nnz < 2^32
+      const uint32_t dmax = __reduce_max_sync(kFull, deg);
+      if (dmax) {
         const uint32_t lo = (uint32_t)vm, hi = (uint32_t)(vm >> 32);
+        uint32_t mlo = 0, mhi = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) {
-          const uint32_t a = __reduce_add_sync(kFull, ((lo >> j) & 1u) ? deg : 0u);
-          const uint32_t c = __reduce_add_sync(kFull, ((hi >> j) & 1u) ? deg : 0u);
-          if (lane == 0) {
-            if (a) atomicAdd(&s_edges[j], (unsigned long long)a);
-            if (c) atomicAdd(&s_edges[32 + j], (unsigned long long)c);
+          const uint32_t a = __ballot_sync(kFull, (lo >> j) & 1u);
+          const uint32_t c = __ballot_sync(kFull, (hi >> j) & 1u);
+          if (lane == (uint32_t)j) {
+            mlo = a;
+            mhi = c;
           }
+        }
+        const int nbits = 32 - __clz(dmax);
+        for (int b = 0; b < nbits; b++) {
+          const uint32_t plane = __ballot_sync(kFull, (deg >> b) & 1u);
+          acc_lo += (unsigned long long)__popc(mlo & plane) << b;
+          acc_hi += (unsigned long long)__popc(mhi & plane) << b;
         }
       }
     }
   }
   if (final) {
+    if (acc_lo) atomicAdd(&s_edges[lane], acc_lo);
+    if (acc_hi) atomicAdd(&s_edges[32 + lane], acc_hi);
     __syncthreads();
     if (threadIdx.x < nl && s_edges[threadIdx.x])
       atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x]);

@@ -101,16 +101,23 @@ struct BlockIndex {
   static constexpr int value = B == 128 ? 0 : B == 256 ? 1 : 2;
 };
 
-// One warp: the learned scheduler's arm for the state's current level, with
-// the model and graph constants held in the state, stored in st->arm for
-// explore_any (and, if sw != 0, set as switch condition sw).  Kept out of line
-// so that the callers' register allocation is not affected.
-__device__ __noinline__ void fused_sched_pick(BfsDevState *st, unsigned long long sw,
-                                              int use_cond) {
+// One warp: the learned scheduler's arm for the state's current level, from
+// the weights w (staged in shared memory by the caller) and the graph
+// constants held in the state, stored in st->arm for explore_any (and, if
+// sw != 0, set as switch condition sw).  Kept out of line so that the
+// callers' register allocation is not affected.
+__device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w,
+                                              unsigned long long sw, int use_cond) {
   SchedGraphConst gc;
   gc.diam = st->sched_diam;
   gc.avg_deg_x = st->sched_avg_deg_x;
-  sched_pick_warp(st, st->sched_w, st->sched_min_conf, gc, sw, use_cond != 0 && sw != 0);
+  sched_pick_warp(st, w, st->sched_min_conf, gc, sw, use_cond != 0 && sw != 0);
+}
+
+// Copies the model to shared memory with all threads of the block: one
+// round of parallel loads instead of the MLP's dependent ones.
+__device__ __forceinline__ void stage_weights(float *dst, const float *__restrict__ w) {
+  for (uint32_t i = threadIdx.x; i < (uint32_t)kSchedParams; i += blockDim.x) dst[i] = w[i];
 }
 
 __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_cond) {
@@ -160,10 +167,13 @@ __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_con
 // One warp: thread 0 seeds the root and the first frontier; with a fused
 // scheduler the warp then picks level 0's arm.
 __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_cond) {
+  __shared__ float s_w[kSchedParams];
   if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const float *w = st->sched_w;
+  if (w != nullptr) stage_weights(s_w, w);
   if (threadIdx.x == 0) init_state(st, cond, use_cond);
   __syncwarp();
-  if (st->sched_w != nullptr) fused_sched_pick(st, st->sched_cond0, use_cond);
+  if (w != nullptr) fused_sched_pick(st, s_w, st->sched_cond0, use_cond);
 }
 
 // ---- explore: LLB / SLB -----------------------------------------------------
@@ -537,6 +547,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
                                                                    int use_cond) {
   constexpr int NW = B / 32;
   constexpr uint32_t kSpan = NW * 32u;  // words per block and step
+  static_assert(kSchedParams <= NW * 32 * 32, "the model must fit the list buffer");
   __shared__ uint32_t s_list[NW][32 * 32];
   __shared__ unsigned long long s_wtot[NW];
   __shared__ unsigned long long s_base;
@@ -671,15 +682,24 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     s_last = (ticket == gridDim.x - 1);
   }
   __syncthreads();
-  if (s_last && warp == 0) {
-    if (lane == 0) {
-      __threadfence();
-      finish_level(st, cond, use_cond);
-    }
-    __syncwarp();
+  if (s_last) {  // uniform over the block
     // fused scheduler: the arm of the level just generated, for the
-    // explore_any launch of the next loop iteration
-    if (st->sched_w != nullptr) fused_sched_pick(st, st->sched_cond, use_cond);
+    // explore_any launch of the next loop iteration; the model goes to the
+    // (now unused) vertex-list buffer first
+    const float *w = st->sched_w;
+    float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
+    if (w != nullptr) {
+      stage_weights(s_w, w);
+      __syncthreads();
+    }
+    if (warp == 0) {
+      if (lane == 0) {
+        __threadfence();
+        finish_level(st, cond, use_cond);
+      }
+      __syncwarp();
+      if (w != nullptr) fused_sched_pick(st, s_w, st->sched_cond, use_cond);
+    }
   }
 }
 

@@ -389,9 +389,9 @@ def run_gb300(a):
         multigraph = {
             "graphs_per_s": round(len(graphs) / (m_ms * 1e-3), 1),
             "launch_ms": round(m_ms, 4),
-            "autotuned": {"block": best[0], "items_per_thread": best[1],
-                          "times_ms": {f"{b}x{p}": round(t, 4)
-                                       for (b, p), t in zip(B.MULTI_CONFIGS, tune_ms)}},
+            "autotuned": {"block": best[0], "items_per_thread": best[1], "cluster": best[2],
+                          "times_ms": {f"{b}x{p}" + (f"c{c}" if c > 1 else ""): round(t, 4)
+                                       for (b, p, c), t in zip(B.MULTI_CONFIGS_ALL, tune_ms)}},
             "sequential_plain_launches_graphs_per_s": round(len(graphs) / (seq_plain * 1e-3), 1),
             "sequential_graph_loop_graphs_per_s": round(len(graphs) / (seq_graph * 1e-3), 1),
             "speedup_vs_sequential_plain_launches": round(seq_plain / m_ms, 2),

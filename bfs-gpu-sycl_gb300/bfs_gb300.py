@@ -147,6 +147,11 @@ def lib():
     _sig(L, "bfs_multi_level_offset", [VP, C.c_uint32, C.POINTER(C.c_uint64)])
     _sig(L, "bfs_multi_run", [VP, U32P, C.c_int32, C.c_int32, VP, C.POINTER(C.c_uint64),
                               C.POINTER(C.c_double)])
+    _sig(L, "bfs_multi_run_ex", [VP, U32P, C.c_int32, C.c_int32, C.c_int32, VP,
+                                 C.POINTER(C.c_uint64), C.POINTER(C.c_double)])
+    _sig(L, "bfs_multi_autotune_ex", [VP, U32P, VP, C.c_int32, C.c_char_p, I32P, I32P, I32P,
+                                      C.POINTER(C.c_float)])
+    _sig(L, "bfs_multi_num_configs", [I32P, I32P, I32P, C.c_int32], C.c_int32)
     _sig(L, "bfs_multi_autotune", [VP, U32P, VP, C.c_int32, C.c_char_p, I32P, I32P,
                                    C.POINTER(C.c_float)])
     _lib = L
@@ -315,6 +320,10 @@ def options(lb="llb", block=256, sm_factor=0, loop="graph", l2_pin=True, record=
 
 
 MULTI_CONFIGS = [(b, p) for b in (128, 256, 512) for p in (1, 2, 4)]
+# (block, ipt, cluster): the single-block configurations, then the clustered
+# ones, in the library's order (bfs_multi_num_configs)
+MULTI_CONFIGS_ALL = [(b, p, 1) for b, p in MULTI_CONFIGS] + \
+    [(b, p, c) for c in (2, 4, 8) for b in (256, 512) for p in (2, 4)]
 
 
 def multi_batch_specs(n=256, first_seed=100, scales=(10, 16), edge_factor=16):
@@ -363,21 +372,32 @@ class MultiBatch:
         check(lib().bfs_multi_level_offset(self.h, g, C.byref(off)))
         return off.value
 
-    def run(self, roots, levels_ptr, block=256, ipt=2):
+    def run(self, roots, levels_ptr, block=256, ipt=2, cluster=1):
+        """One launch over the batch; cluster > 1 runs the largest graphs on
+        clusters of that many thread blocks."""
         rt = np.ascontiguousarray(roots, np.uint32)
         ec = np.zeros(self.n_graphs, np.uint64)
         ms = C.c_double(0)
-        check(lib().bfs_multi_run(self.h, rt.ctypes.data_as(U32P), block, ipt, VP(levels_ptr),
-                                  ec.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(ms)))
+        check(lib().bfs_multi_run_ex(self.h, rt.ctypes.data_as(U32P), block, ipt, cluster,
+                                     VP(levels_ptr), ec.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                     C.byref(ms)))
         return ec, ms.value
 
-    def autotune(self, roots, levels_ptr, reps=3, cache_path=None):
+    def autotune(self, roots, levels_ptr, reps=3, cache_path=None, clusters=True):
+        """Fastest configuration on this batch: (block, ipt, cluster) and the
+        timings of MULTI_CONFIGS_ALL (clusters=True), else (block, ipt) and
+        the timings of MULTI_CONFIGS."""
         rt = np.ascontiguousarray(roots, np.uint32)
-        b, p = C.c_int32(0), C.c_int32(0)
+        b, p, c = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        cp = cache_path.encode() if cache_path else None
+        if clusters:
+            t = (C.c_float * len(MULTI_CONFIGS_ALL))()
+            check(lib().bfs_multi_autotune_ex(self.h, rt.ctypes.data_as(U32P), VP(levels_ptr),
+                                              reps, cp, C.byref(b), C.byref(p), C.byref(c), t))
+            return (b.value, p.value, c.value), list(t)
         t = (C.c_float * len(MULTI_CONFIGS))()
         check(lib().bfs_multi_autotune(self.h, rt.ctypes.data_as(U32P), VP(levels_ptr), reps,
-                                       cache_path.encode() if cache_path else None, C.byref(b),
-                                       C.byref(p), t))
+                                       cp, C.byref(b), C.byref(p), t))
         return (b.value, p.value), list(t)
 
     def free(self):

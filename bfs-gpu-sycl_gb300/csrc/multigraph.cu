@@ -18,6 +18,7 @@
 // from an autotuner that times every combination on the batch and caches the
 // choice per GPU and batch shape.  The launch (work-counter reset, level fill,
 // persistent kernel) is captured once into a CUDA graph and replayed.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -45,130 +46,279 @@ struct MultiDesc {
   uint32_t pad;
 };
 
-template <int B, int IPT>
-__global__ void __launch_bounds__(B) multi_bfs_kernel(const MultiDesc *__restrict__ descs,
-                                                      const uint32_t *__restrict__ order,
-                                                      uint32_t n_graphs,
-                                                      const uint32_t *__restrict__ indptr_all,
-                                                      const uint32_t *__restrict__ inds_all,
-                                                      uint32_t *work, uint32_t *queues,
-                                                      uint32_t qcap, int32_t *levels,
-                                                      unsigned long long *edges_out) {
+// Kernel parameters (passed by value).
+struct MultiArgs {
+  const MultiDesc *descs;
+  const uint32_t *order;        // graphs, largest edge count first
+  uint32_t n_graphs;
+  uint32_t n_big;               // order[0, n_big): graphs run by a whole cluster
+  const uint32_t *indptr_all;
+  const uint32_t *inds_all;
+  uint32_t *work;               // [0]: next small graph, [1]: next big graph
+  uint32_t *queues;             // two queues of qcap entries per block
+  uint32_t qcap;
+  uint32_t *gbits;              // per cluster: the authoritative visited bitmap
+  uint32_t gwords;              // words per cluster bitmap
+  uint32_t *gcnt;               // per cluster: 3 queue counters + claimed graph
+  int32_t *levels;
+  unsigned long long *edges_out;
+};
+
+// One level of one graph over tiles tile0, tile0 + tstride, ... of B
+// frontier entries (LLB form): block exclusive scan of the tile's degrees,
+// the tile's edges split evenly over the warps, owners resolved per warp
+// round, IPT rounds in flight per lane.  A claim is an atomicOr on the
+// visited bitmap -- the block's own shared bitmap, or, for a graph shared by
+// a cluster (CL), the cluster's bitmap in global memory, with the shared
+// bitmap kept as a filter of already visited vertices.  The claiming thread
+// writes the level; kept vertices are appended to qn with one atomic per warp
+// round on *ctr.  Returns (in thread 0) the sum of the tiles' degrees.
+template <int B, int IPT, bool CL>
+__device__ __forceinline__ unsigned long long multi_level(
+    const uint32_t *__restrict__ ip, const uint32_t *__restrict__ ix, int32_t *lv,
+    uint32_t n_rows, const uint32_t *qc, uint32_t *qn, uint32_t F, int32_t lvl,
+    uint32_t tile0, uint32_t tstride, uint32_t *s_bitmap, uint32_t *gb, uint32_t *ctr,
+    uint32_t *s_off, uint32_t *s_beg, uint32_t *s_wsum) {
   constexpr int NW = B / 32;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  unsigned long long edges = 0;
+  for (uint32_t tile = tile0; tile < F; tile += tstride) {
+    const uint32_t slot = tile + threadIdx.x;
+    uint32_t beg = 0, deg = 0;
+    if (slot < F) {
+      const uint32_t u = CL ? __ldcg(qc + slot) : qc[slot];
+      beg = ip[u];
+      deg = ip[u + 1] - beg;
+    }
+    const uint32_t incl = warp_incl_scan(deg, lane);
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < (uint32_t)NW ? s_wsum[lane] : 0u;
+      w = warp_incl_scan(w, lane);
+      if (lane < (uint32_t)NW) s_wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t total = s_wsum[NW - 1];
+    s_off[threadIdx.x] = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
+    s_beg[threadIdx.x] = beg;
+    if (threadIdx.x == 0) s_off[B] = total;
+    __syncthreads();
+    const uint32_t per_warp = ((total + NW - 1) / NW + 31u) & ~31u;
+    const uint32_t w0 = warp * per_warp;
+    if (w0 < total) {
+      const uint32_t w1 = min(total, w0 + per_warp);
+      uint32_t lo = 0, hi = B;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_off[mid] <= w0) lo = mid; else hi = mid;
+      }
+      uint32_t cur = lo;
+      for (uint32_t base = w0; base < w1; base += 32u * IPT) {
+        uint32_t addr[IPT];
+#pragma unroll
+        for (int u = 0; u < IPT; u++) {
+          const uint32_t rb = base + 32u * u;
+          const uint32_t e = rb + lane;
+          const uint32_t j = cur + 1u + lane;
+          const uint32_t bnd = (j <= (uint32_t)B) ? s_off[j] : kFull;
+          const uint32_t p = bnd - rb;
+          const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
+          const uint32_t o = cur + __popc(starts & ((2u << lane) - 1u));
+          addr[u] = (e < w1) ? s_beg[o] + (e - s_off[o]) : kFull;
+          cur = __shfl_sync(kFull, o, 31);
+          if (cur >= (uint32_t)B) cur = B - 1;
+        }
+        uint32_t nb[IPT];
+#pragma unroll
+        for (int u = 0; u < IPT; u++) nb[u] = addr[u] != kFull ? ix[addr[u]] : 0u;
+#pragma unroll
+        for (int u = 0; u < IPT; u++) {
+          bool push = false;
+          const uint32_t v = nb[u];
+          if (addr[u] != kFull) {
+            const uint32_t w = v >> 5, bit = 1u << (v & 31u);
+            if (!(s_bitmap[w] & bit)) {
+              uint32_t old;
+              if (CL) {
+                old = atomicOr(gb + w, bit);
+                atomicOr(s_bitmap + w, bit);
+              } else {
+                old = atomicOr(s_bitmap + w, bit);
+              }
+              if (!(old & bit)) {
+                lv[v] = lvl + 1;
+                push = v < n_rows && ip[v + 1] > ip[v];
+              }
+            }
+          }
+          const uint32_t pm = __ballot_sync(kFull, push);
+          if (pm) {
+            const uint32_t leader = __ffs(pm) - 1u;
+            uint32_t base0 = 0;
+            if (lane == leader) base0 = atomicAdd(ctr, (uint32_t)__popc(pm));
+            base0 = __shfl_sync(kFull, base0, leader);
+            if (push) qn[base0 + __popc(pm & lt_mask)] = v;
+          }
+        }
+      }
+    }
+    if (threadIdx.x == 0) edges += total;
+    __syncthreads();
+  }
+  return edges;
+}
+
+// A complete BFS of one graph by one block, the visited bitmap in shared
+// memory and __syncthreads as the level barrier.
+template <int B, int IPT>
+__device__ __forceinline__ void multi_graph_block(const MultiArgs &a, uint32_t gi,
+                                                  uint32_t *s_bitmap, uint32_t *s_off,
+                                                  uint32_t *s_beg, uint32_t *s_wsum,
+                                                  uint32_t *s_next) {
+  const MultiDesc d = a.descs[a.order[gi]];
+  const uint32_t *__restrict__ ip = a.indptr_all + d.vbase;
+  const uint32_t *__restrict__ ix = a.inds_all + d.ebase;
+  int32_t *lv = a.levels + d.lbase;
+  uint32_t *q0 = a.queues + (size_t)blockIdx.x * 2 * a.qcap;
+  uint32_t *q1 = q0 + a.qcap;
+  const uint32_t words = (d.n_cols + 31u) >> 5;
+  for (uint32_t w = threadIdx.x; w < words; w += B) s_bitmap[w] = 0u;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t r = d.root;
+    s_bitmap[r >> 5] |= 1u << (r & 31u);
+    lv[r] = 0;
+    const uint32_t rdeg = r < d.n_rows ? ip[r + 1] - ip[r] : 0u;
+    if (rdeg) q0[0] = r;
+    s_next[0] = rdeg ? 1u : 0u;
+  }
+  __syncthreads();
+  uint32_t F = s_next[0];
+  uint32_t *qc = q0, *qn = q1;
+  unsigned long long edges = 0;
+  int32_t lvl = 0;
+  while (F > 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_next[0] = 0;
+    __syncthreads();
+    edges += multi_level<B, IPT, false>(ip, ix, lv, d.n_rows, qc, qn, F, lvl, 0u, B, s_bitmap,
+                                        nullptr, s_next, s_off, s_beg, s_wsum);
+    __syncthreads();
+    F = s_next[0];
+    uint32_t *t = qc;
+    qc = qn;
+    qn = t;
+    lvl++;
+  }
+  if (threadIdx.x == 0) a.edges_out[a.order[gi]] = edges;
+}
+
+// Graphs claimed one per block from a work counter (largest first).
+template <int B, int IPT>
+__device__ __forceinline__ void multi_small_graphs(const MultiArgs &a, uint32_t *s_bitmap,
+                                                   uint32_t *s_off, uint32_t *s_beg,
+                                                   uint32_t *s_wsum, uint32_t *s_next,
+                                                   uint32_t *s_graph) {
+  for (;;) {
+    if (threadIdx.x == 0) *s_graph = a.n_big + atomicAdd(&a.work[0], 1u);
+    __syncthreads();
+    const uint32_t gi = *s_graph;
+    if (gi >= a.n_graphs) break;
+    multi_graph_block<B, IPT>(a, gi, s_bitmap, s_off, s_beg, s_wsum, s_next);
+    __syncthreads();
+  }
+}
+
+template <int B, int IPT>
+__global__ void __launch_bounds__(B) multi_bfs_kernel(MultiArgs a) {
   extern __shared__ uint32_t s_bitmap[];
   __shared__ uint32_t s_off[B + 1];
   __shared__ uint32_t s_beg[B];
-  __shared__ uint32_t s_wsum[NW];
-  __shared__ uint32_t s_graph, s_next;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  uint32_t *q0 = queues + (size_t)blockIdx.x * 2 * qcap;
-  uint32_t *q1 = q0 + qcap;
+  __shared__ uint32_t s_wsum[B / 32];
+  __shared__ uint32_t s_next[1], s_graph[1];
+  multi_small_graphs<B, IPT>(a, s_bitmap, s_off, s_beg, s_wsum, s_next, s_graph);
+}
 
+// Clusters of C blocks first share the largest graphs (order[0, n_big)): a
+// claimed graph's frontier tiles are dealt round-robin over the cluster's
+// blocks, claims go to the cluster's bitmap in global memory (L2), every
+// block keeps a shared-memory copy of the visited set as a filter (merged
+// from the new frontier after every level), the level barrier is the
+// cluster barrier, and the next frontier is one queue per cluster with
+// counters in global memory.  Then every block takes small graphs on its
+// own.  Each frontier entry is expanded by exactly one block, so the edge
+// counts stay exact.
+template <int B, int IPT, int C>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(B)
+    multi_bfs_cluster_kernel(MultiArgs a) {
+  extern __shared__ uint32_t s_bitmap[];
+  __shared__ uint32_t s_off[B + 1];
+  __shared__ uint32_t s_beg[B];
+  __shared__ uint32_t s_wsum[B / 32];
+  __shared__ uint32_t s_next[1], s_graph[1];
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t rank = cl.block_rank();
+  const uint32_t cid = blockIdx.x / C;
+  uint32_t *gb = a.gbits + (size_t)cid * a.gwords;
+  uint32_t *cnt = a.gcnt + (size_t)cid * 4;
+  uint32_t *cq0 = a.queues + (size_t)(blockIdx.x - rank) * 2 * a.qcap;
+  uint32_t *cq1 = cq0 + a.qcap;
   for (;;) {
-    if (threadIdx.x == 0) s_graph = atomicAdd(work, 1u);
-    __syncthreads();
-    const uint32_t gi = s_graph;
-    if (gi >= n_graphs) break;
-    const MultiDesc d = descs[order[gi]];
-    const uint32_t *__restrict__ ip = indptr_all + d.vbase;
-    const uint32_t *__restrict__ ix = inds_all + d.ebase;
-    int32_t *lv = levels + d.lbase;
+    if (rank == 0 && threadIdx.x == 0) {
+      cnt[3] = atomicAdd(&a.work[1], 1u);
+      cnt[0] = cnt[1] = cnt[2] = 0;
+    }
+    cl.sync();
+    const uint32_t gi = __ldcg(cnt + 3);
+    if (gi >= a.n_big) break;  // uniform over the cluster
+    const MultiDesc d = a.descs[a.order[gi]];
+    const uint32_t *__restrict__ ip = a.indptr_all + d.vbase;
+    const uint32_t *__restrict__ ix = a.inds_all + d.ebase;
+    int32_t *lv = a.levels + d.lbase;
     const uint32_t words = (d.n_cols + 31u) >> 5;
+    for (uint32_t w = rank * B + threadIdx.x; w < words; w += C * B) gb[w] = 0u;
     for (uint32_t w = threadIdx.x; w < words; w += B) s_bitmap[w] = 0u;
-    __syncthreads();
-    unsigned long long edges = 0;  // sum of the degrees of every expanded tile
-    uint32_t F = 0;
-    if (threadIdx.x == 0) {
-      const uint32_t r = d.root;
-      s_bitmap[r >> 5] |= 1u << (r & 31u);
+    cl.sync();
+    const uint32_t r = d.root;
+    if (threadIdx.x == 0) s_bitmap[r >> 5] |= 1u << (r & 31u);
+    if (rank == 0 && threadIdx.x == 0) {
+      gb[r >> 5] |= 1u << (r & 31u);
       lv[r] = 0;
       const uint32_t rdeg = r < d.n_rows ? ip[r + 1] - ip[r] : 0u;
-      if (rdeg) q0[0] = r;
-      s_next = rdeg ? 1u : 0u;
+      if (rdeg) cq0[0] = r;
+      cnt[0] = rdeg ? 1u : 0u;
     }
-    __syncthreads();
-    F = s_next;
-    uint32_t *qc = q0, *qn = q1;
+    cl.sync();
+    uint32_t F = __ldcg(cnt + 0);
+    unsigned long long edges = 0;
     int32_t lvl = 0;
     while (F > 0) {
-      __syncthreads();
-      if (threadIdx.x == 0) s_next = 0;
-      __syncthreads();
-      for (uint32_t tile = 0; tile < F; tile += B) {
-        const uint32_t slot = tile + threadIdx.x;
-        uint32_t beg = 0, deg = 0;
-        if (slot < F) {
-          const uint32_t u = qc[slot];
-          beg = ip[u];
-          deg = ip[u + 1] - beg;
-        }
-        const uint32_t incl = warp_incl_scan(deg, lane);
-        if (lane == 31) s_wsum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-          uint32_t w = lane < (uint32_t)NW ? s_wsum[lane] : 0u;
-          w = warp_incl_scan(w, lane);
-          if (lane < (uint32_t)NW) s_wsum[lane] = w;
-        }
-        __syncthreads();
-        const uint32_t total = s_wsum[NW - 1];
-        s_off[threadIdx.x] = (warp ? s_wsum[warp - 1] : 0u) + incl - deg;
-        s_beg[threadIdx.x] = beg;
-        if (threadIdx.x == 0) s_off[B] = total;
-        __syncthreads();
-        const uint32_t per_warp = ((total + NW - 1) / NW + 31u) & ~31u;
-        const uint32_t w0 = warp * per_warp;
-        if (w0 < total) {
-          const uint32_t w1 = min(total, w0 + per_warp);
-          uint32_t lo = 0, hi = B;
-          while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_off[mid] <= w0) lo = mid; else hi = mid;
-          }
-          uint32_t cur = lo;
-          for (uint32_t base = w0; base < w1; base += 32u * IPT) {
-            uint32_t addr[IPT];
-#pragma unroll
-            for (int u = 0; u < IPT; u++) {
-              const uint32_t rb = base + 32u * u;
-              const uint32_t e = rb + lane;
-              const uint32_t j = cur + 1u + lane;
-              const uint32_t bnd = (j <= (uint32_t)B) ? s_off[j] : kFull;
-              const uint32_t p = bnd - rb;
-              const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
-              const uint32_t o = cur + __popc(starts & ((2u << lane) - 1u));
-              addr[u] = (e < w1) ? s_beg[o] + (e - s_off[o]) : kFull;
-              cur = __shfl_sync(kFull, o, 31);
-              if (cur >= (uint32_t)B) cur = B - 1;
-            }
-            uint32_t nb[IPT];
-#pragma unroll
-            for (int u = 0; u < IPT; u++) nb[u] = addr[u] != kFull ? ix[addr[u]] : 0u;
-#pragma unroll
-            for (int u = 0; u < IPT; u++) {
-              if (addr[u] == kFull) continue;
-              const uint32_t v = nb[u], bit = 1u << (v & 31u);
-              if (s_bitmap[v >> 5] & bit) continue;
-              const uint32_t old = atomicOr(&s_bitmap[v >> 5], bit);
-              if (old & bit) continue;
-              lv[v] = lvl + 1;
-              if (v < d.n_rows && ip[v + 1] > ip[v]) qn[atomicAdd(&s_next, 1u)] = v;
-            }
-          }
-        }
-        if (threadIdx.x == 0) edges += total;
-        __syncthreads();
+      // counter (lvl + 2) % 3 held a frontier size that everyone read
+      // before the previous barrier; it takes the appends of level lvl + 1
+      if (rank == 0 && threadIdx.x == 0) cnt[(lvl + 2) % 3] = 0;
+      uint32_t *qc = (lvl & 1) ? cq1 : cq0;
+      uint32_t *qn = (lvl & 1) ? cq0 : cq1;
+      uint32_t *ctr = cnt + (lvl + 1) % 3;
+      edges += multi_level<B, IPT, true>(ip, ix, lv, d.n_rows, qc, qn, F, lvl, rank * B, C * B,
+                                         s_bitmap, gb, ctr, s_off, s_beg, s_wsum);
+      cl.sync();
+      const uint32_t fn = __ldcg(ctr);
+      // vertices claimed by the other blocks join this block's filter
+      for (uint32_t i = threadIdx.x; i < fn; i += B) {
+        const uint32_t v = __ldcg(qn + i);
+        atomicOr(s_bitmap + (v >> 5), 1u << (v & 31u));
       }
       __syncthreads();
-      F = s_next;
-      uint32_t *t = qc;
-      qc = qn;
-      qn = t;
+      F = fn;
       lvl++;
     }
-    if (threadIdx.x == 0) edges_out[order[gi]] = edges;
-    __syncthreads();
+    if (threadIdx.x == 0 && edges) atomicAdd(&a.edges_out[a.order[gi]], edges);
+    cl.sync();  // queues, counters and bitmap are free for the cluster's next graph
   }
+  multi_small_graphs<B, IPT>(a, s_bitmap, s_off, s_beg, s_wsum, s_next, s_graph);
 }
 
 __global__ void multi_fill_kernel(int32_t *levels, uint64_t n) {
@@ -177,23 +327,28 @@ __global__ void multi_fill_kernel(int32_t *levels, uint64_t n) {
     levels[i] = -1;
 }
 
-using MultiKernel = void (*)(const MultiDesc *, const uint32_t *, uint32_t, const uint32_t *,
-                             const uint32_t *, uint32_t *, uint32_t *, uint32_t, int32_t *,
-                             unsigned long long *);
+using MultiKernel = void (*)(MultiArgs);
 
 struct MultiConfig {
-  int block, ipt;
+  int block, ipt, cluster;
   MultiKernel fn;
 };
 
 static const MultiConfig kMultiConfigs[] = {
-    {128, 1, multi_bfs_kernel<128, 1>}, {128, 2, multi_bfs_kernel<128, 2>},
-    {128, 4, multi_bfs_kernel<128, 4>}, {256, 1, multi_bfs_kernel<256, 1>},
-    {256, 2, multi_bfs_kernel<256, 2>}, {256, 4, multi_bfs_kernel<256, 4>},
-    {512, 1, multi_bfs_kernel<512, 1>}, {512, 2, multi_bfs_kernel<512, 2>},
-    {512, 4, multi_bfs_kernel<512, 4>},
+    {128, 1, 1, multi_bfs_kernel<128, 1>}, {128, 2, 1, multi_bfs_kernel<128, 2>},
+    {128, 4, 1, multi_bfs_kernel<128, 4>}, {256, 1, 1, multi_bfs_kernel<256, 1>},
+    {256, 2, 1, multi_bfs_kernel<256, 2>}, {256, 4, 1, multi_bfs_kernel<256, 4>},
+    {512, 1, 1, multi_bfs_kernel<512, 1>}, {512, 2, 1, multi_bfs_kernel<512, 2>},
+    {512, 4, 1, multi_bfs_kernel<512, 4>},
+    {256, 2, 2, multi_bfs_cluster_kernel<256, 2, 2>}, {256, 4, 2, multi_bfs_cluster_kernel<256, 4, 2>},
+    {512, 2, 2, multi_bfs_cluster_kernel<512, 2, 2>}, {512, 4, 2, multi_bfs_cluster_kernel<512, 4, 2>},
+    {256, 2, 4, multi_bfs_cluster_kernel<256, 2, 4>}, {256, 4, 4, multi_bfs_cluster_kernel<256, 4, 4>},
+    {512, 2, 4, multi_bfs_cluster_kernel<512, 2, 4>}, {512, 4, 4, multi_bfs_cluster_kernel<512, 4, 4>},
+    {256, 2, 8, multi_bfs_cluster_kernel<256, 2, 8>}, {256, 4, 8, multi_bfs_cluster_kernel<256, 4, 8>},
+    {512, 2, 8, multi_bfs_cluster_kernel<512, 2, 8>}, {512, 4, 8, multi_bfs_cluster_kernel<512, 4, 8>},
 };
 constexpr int kNumMultiConfigs = sizeof(kMultiConfigs) / sizeof(kMultiConfigs[0]);
+constexpr int kNumSingleConfigs = 9;  // the first 9: one block per graph
 
 }  // namespace bfsgb
 
@@ -208,6 +363,10 @@ struct bfs_multi {
   std::vector<MultiDesc> descs;
   uint32_t *d_indptr = nullptr, *d_inds = nullptr, *d_order = nullptr, *d_work = nullptr;
   uint32_t *d_queues = nullptr;
+  uint32_t *d_gbits = nullptr, *d_gcnt = nullptr;  // cluster bitmaps and counters
+  size_t gbits_words = 0, gcnt_words = 0;
+  std::vector<uint64_t> order_nnz;                   // edge counts in claim order
+  uint32_t n_big = 0;
   MultiDesc *d_descs = nullptr;
   unsigned long long *d_edges = nullptr;
   size_t queue_blocks = 0;
@@ -229,9 +388,11 @@ struct bfs_multi {
                   std::string(#call) + ": " + cudaGetErrorString(e_));             \
   } while (0)
 
-static int config_index(int block, int ipt) {
+static int config_index(int block, int ipt, int cluster) {
   for (int i = 0; i < kNumMultiConfigs; i++)
-    if (kMultiConfigs[i].block == block && kMultiConfigs[i].ipt == ipt) return i;
+    if (kMultiConfigs[i].block == block && kMultiConfigs[i].ipt == ipt &&
+        kMultiConfigs[i].cluster == cluster)
+      return i;
   return -1;
 }
 
@@ -242,22 +403,61 @@ static bfs_status multi_prepare(bfs_multi *m, int cfg, int32_t *levels_dev) {
   m->exec = nullptr;
   m->graph = nullptr;
   const MultiConfig &c = kMultiConfigs[cfg];
-  const size_t smem = (size_t)((m->max_cols + 31) / 32) * 4;
+  const uint32_t words = (m->max_cols + 31) / 32;
+  const size_t smem = (size_t)words * 4;
   GK(cudaFuncSetAttribute((const void *)c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)std::max<size_t>(smem, 1)));
   int occ = 0;
   GK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)c.fn, c.block, smem));
   int grid = m->num_sms * std::max(occ, 1);
   grid = (int)std::min<size_t>((size_t)grid, m->queue_blocks);
-  grid = std::max(1, std::min<int>(grid, (int)m->n_graphs));
+  uint32_t n_big = 0;
+  if (c.cluster > 1) {
+    grid = std::max(c.cluster, grid / c.cluster * c.cluster);
+    // a graph is shared by a cluster when its edges exceed `cluster` blocks'
+    // fair share of the batch's edges
+    for (uint32_t i = 0; i < m->n_graphs; i++)
+      if ((double)m->order_nnz[i] * grid >= (double)m->total_edges * c.cluster) n_big = i + 1;
+    const size_t n_clusters = (size_t)grid / c.cluster;
+    if (m->gbits_words < n_clusters * words) {
+      cudaFree(m->d_gbits);
+      m->d_gbits = nullptr;
+      GK(cudaMalloc(&m->d_gbits, sizeof(uint32_t) * n_clusters * words));
+      m->gbits_words = n_clusters * words;
+    }
+    if (m->gcnt_words < n_clusters * 4) {
+      cudaFree(m->d_gcnt);
+      m->d_gcnt = nullptr;
+      GK(cudaMalloc(&m->d_gcnt, sizeof(uint32_t) * n_clusters * 4));
+      m->gcnt_words = n_clusters * 4;
+    }
+  } else {
+    grid = std::max(1, std::min<int>(grid, (int)m->n_graphs));
+  }
   m->grid = grid;
-  // capture: reset work counter, fill levels with -1, persistent kernel
+  m->n_big = n_big;
+  MultiArgs a;
+  a.descs = m->d_descs;
+  a.order = m->d_order;
+  a.n_graphs = m->n_graphs;
+  a.n_big = n_big;
+  a.indptr_all = m->d_indptr;
+  a.inds_all = m->d_inds;
+  a.work = m->d_work;
+  a.queues = m->d_queues;
+  a.qcap = m->max_rows;
+  a.gbits = m->d_gbits;
+  a.gwords = words;
+  a.gcnt = m->d_gcnt;
+  a.levels = levels_dev;
+  a.edges_out = m->d_edges;
+  // capture: reset the work counters and edge counts, fill levels with -1,
+  // persistent kernel
   GK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(m->d_work, 0, sizeof(uint32_t), m->stream);
+  cudaMemsetAsync(m->d_work, 0, 2 * sizeof(uint32_t), m->stream);
+  cudaMemsetAsync(m->d_edges, 0, sizeof(unsigned long long) * m->n_graphs, m->stream);
   multi_fill_kernel<<<m->num_sms * 4, 256, 0, m->stream>>>(levels_dev, m->total_cols);
-  c.fn<<<grid, c.block, smem, m->stream>>>(m->d_descs, m->d_order, m->n_graphs, m->d_indptr,
-                                           m->d_inds, m->d_work, m->d_queues, m->max_rows,
-                                           levels_dev, m->d_edges);
+  c.fn<<<grid, c.block, smem, m->stream>>>(a);
   cudaError_t ce = cudaStreamEndCapture(m->stream, &m->graph);
   if (ce != cudaSuccess)
     return fail(BFS_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
@@ -311,6 +511,8 @@ bfs_status bfs_multi_create(uint32_t n_graphs, const uint32_t *const *indptrs,
   std::iota(order.begin(), order.end(), 0u);
   std::stable_sort(order.begin(), order.end(),
                    [&](uint32_t a, uint32_t b) { return nnz[a] > nnz[b]; });
+  m->order_nnz.resize(n_graphs);
+  for (uint32_t i = 0; i < n_graphs; i++) m->order_nnz[i] = nnz[order[i]];
   bfs_status rc = BFS_OK;
   std::vector<uint32_t> hip(vb), hix(eb ? eb : 1);
   for (uint32_t g = 0; g < n_graphs; g++) {
@@ -361,7 +563,7 @@ bfs_status bfs_multi_create(uint32_t n_graphs, const uint32_t *const *indptrs,
   CK2(cudaMalloc(&m->d_indptr, sizeof(uint32_t) * vb));
   CK2(cudaMalloc(&m->d_inds, sizeof(uint32_t) * std::max<uint64_t>(eb, 1)));
   CK2(cudaMalloc(&m->d_order, sizeof(uint32_t) * n_graphs));
-  CK2(cudaMalloc(&m->d_work, sizeof(uint32_t)));
+  CK2(cudaMalloc(&m->d_work, 2 * sizeof(uint32_t)));
   CK2(cudaMalloc(&m->d_descs, sizeof(MultiDesc) * n_graphs));
   CK2(cudaMalloc(&m->d_edges, sizeof(unsigned long long) * n_graphs));
   // queues: two of max_rows entries per resident block (bounded by the
@@ -388,6 +590,8 @@ bfs_status bfs_multi_free(bfs_multi *m) {
   cudaFree(m->d_order);
   cudaFree(m->d_work);
   cudaFree(m->d_queues);
+  cudaFree(m->d_gbits);
+  cudaFree(m->d_gcnt);
   cudaFree(m->d_descs);
   cudaFree(m->d_edges);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -405,9 +609,18 @@ bfs_status bfs_multi_level_offset(const bfs_multi *m, uint32_t graph, uint64_t *
 
 bfs_status bfs_multi_run(bfs_multi *m, const uint32_t *roots, int32_t block, int32_t ipt,
                          int32_t *levels_dev, uint64_t *edges_count_out, double *device_ms) {
+  return bfs_multi_run_ex(m, roots, block, ipt, 1, levels_dev, edges_count_out, device_ms);
+}
+
+bfs_status bfs_multi_run_ex(bfs_multi *m, const uint32_t *roots, int32_t block, int32_t ipt,
+                            int32_t cluster, int32_t *levels_dev, uint64_t *edges_count_out,
+                            double *device_ms) {
   if (!m || !roots || !levels_dev) return fail(BFS_ERR_INVALID_ARG, "null pointer");
-  const int cfg = config_index(block, ipt);
-  if (cfg < 0) return fail(BFS_ERR_INVALID_ARG, "block must be 128/256/512 and ipt 1/2/4");
+  const int cfg = config_index(block, ipt, cluster);
+  if (cfg < 0)
+    return fail(BFS_ERR_INVALID_ARG,
+                "unsupported configuration: block 128/256/512 x ipt 1/2/4 (cluster 1), or "
+                "block 256/512 x ipt 2/4 x cluster 2/4/8");
   for (uint32_t g = 0; g < m->n_graphs; g++)
     if (roots[g] >= m->descs[g].n_cols) return fail(BFS_ERR_ROOT, "root out of range");
   GK(cudaSetDevice(m->device));
@@ -434,45 +647,49 @@ bfs_status bfs_multi_run(bfs_multi *m, const uint32_t *roots, int32_t block, int
   return BFS_OK;
 }
 
-bfs_status bfs_multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
-                              int32_t reps, const char *cache_path, int32_t *best_block,
-                              int32_t *best_ipt, float *times_ms) {
-  if (!m || !roots || !levels_dev || !best_block || !best_ipt)
-    return fail(BFS_ERR_INVALID_ARG, "null pointer");
+}  // extern "C"
+
+// Times configurations [0, n_cfg) on the batch (best of reps after a warm-up
+// run that also captures the launch) and returns the fastest; a cache file
+// keeps the choice per GPU, batch shape and configuration set.
+static bfs_status multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
+                                 int32_t reps, const char *cache_path, int n_cfg, int *best_out,
+                                 float *times_ms) {
+  if (!m || !roots || !levels_dev) return fail(BFS_ERR_INVALID_ARG, "null pointer");
   if (reps < 1) reps = 3;
   cudaDeviceProp prop;
   GK(cudaGetDeviceProperties(&prop, m->device));
   std::ostringstream key;
   key << prop.name << "|sm" << prop.multiProcessorCount << "|g" << m->n_graphs << "|v"
-      << m->total_cols << "|e" << m->total_edges;
+      << m->total_cols << "|e" << m->total_edges << "|c" << n_cfg;
   if (cache_path && cache_path[0]) {
     std::ifstream in(cache_path);
     std::string line;
     while (std::getline(in, line)) {
-      const size_t t1 = line.rfind('\t');
-      if (t1 == std::string::npos) continue;
-      const size_t t0 = line.rfind('\t', t1 - 1);
-      if (t0 == std::string::npos || line.substr(0, t0) != key.str()) continue;
-      const int b = std::atoi(line.c_str() + t0 + 1), p = std::atoi(line.c_str() + t1 + 1);
-      if (config_index(b, p) >= 0) {
-        *best_block = b;
-        *best_ipt = p;
+      std::istringstream ls(line);
+      std::string k;
+      int b = 0, p = 0, c = 0;
+      if (!std::getline(ls, k, '\t') || k != key.str()) continue;
+      if (!(ls >> b >> p >> c)) continue;
+      const int i = config_index(b, p, c);
+      if (i >= 0 && i < n_cfg) {
+        *best_out = i;
         if (times_ms)
-          for (int i = 0; i < kNumMultiConfigs; i++) times_ms[i] = -1.f;
+          for (int j = 0; j < n_cfg; j++) times_ms[j] = -1.f;
         return BFS_OK;
       }
     }
   }
   int best = 0;
   float best_ms = 1e30f;
-  for (int i = 0; i < kNumMultiConfigs; i++) {
+  for (int i = 0; i < n_cfg; i++) {
+    const MultiConfig &c = kMultiConfigs[i];
     double t = 0.0, mn = 1e30;
-    bfs_status rc = bfs_multi_run(m, roots, kMultiConfigs[i].block, kMultiConfigs[i].ipt,
-                                  levels_dev, nullptr, &t);  // warm-up + capture
+    bfs_status rc = bfs_multi_run_ex(m, roots, c.block, c.ipt, c.cluster, levels_dev, nullptr,
+                                     &t);  // warm-up + capture
     if (rc != BFS_OK) return rc;
     for (int r = 0; r < reps; r++) {
-      rc = bfs_multi_run(m, roots, kMultiConfigs[i].block, kMultiConfigs[i].ipt, levels_dev,
-                         nullptr, &t);
+      rc = bfs_multi_run_ex(m, roots, c.block, c.ipt, c.cluster, levels_dev, nullptr, &t);
       if (rc != BFS_OK) return rc;
       mn = std::min(mn, t);
     }
@@ -482,13 +699,52 @@ bfs_status bfs_multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *leve
       best = i;
     }
   }
-  *best_block = kMultiConfigs[best].block;
-  *best_ipt = kMultiConfigs[best].ipt;
+  *best_out = best;
   if (cache_path && cache_path[0]) {
     std::ofstream outf(cache_path, std::ios::app);
-    if (outf) outf << key.str() << '\t' << *best_block << '\t' << *best_ipt << '\n';
+    if (outf)
+      outf << key.str() << '\t' << kMultiConfigs[best].block << ' ' << kMultiConfigs[best].ipt
+           << ' ' << kMultiConfigs[best].cluster << '\n';
   }
   return BFS_OK;
+}
+
+extern "C" {
+
+bfs_status bfs_multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
+                              int32_t reps, const char *cache_path, int32_t *best_block,
+                              int32_t *best_ipt, float *times_ms) {
+  if (!best_block || !best_ipt) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  int best = 0;
+  bfs_status rc = multi_autotune(m, roots, levels_dev, reps, cache_path, kNumSingleConfigs,
+                                 &best, times_ms);
+  if (rc != BFS_OK) return rc;
+  *best_block = kMultiConfigs[best].block;
+  *best_ipt = kMultiConfigs[best].ipt;
+  return BFS_OK;
+}
+
+bfs_status bfs_multi_autotune_ex(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
+                                 int32_t reps, const char *cache_path, int32_t *best_block,
+                                 int32_t *best_ipt, int32_t *best_cluster, float *times_ms) {
+  if (!best_block || !best_ipt || !best_cluster) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  int best = 0;
+  bfs_status rc = multi_autotune(m, roots, levels_dev, reps, cache_path, kNumMultiConfigs,
+                                 &best, times_ms);
+  if (rc != BFS_OK) return rc;
+  *best_block = kMultiConfigs[best].block;
+  *best_ipt = kMultiConfigs[best].ipt;
+  *best_cluster = kMultiConfigs[best].cluster;
+  return BFS_OK;
+}
+
+int32_t bfs_multi_num_configs(int32_t *blocks, int32_t *ipts, int32_t *clusters, int32_t max) {
+  for (int i = 0; i < kNumMultiConfigs && i < max; i++) {
+    if (blocks) blocks[i] = kMultiConfigs[i].block;
+    if (ipts) ipts[i] = kMultiConfigs[i].ipt;
+    if (clusters) clusters[i] = kMultiConfigs[i].cluster;
+  }
+  return kNumMultiConfigs;
 }
 
 }  // extern "C"

@@ -203,6 +203,24 @@ bfs_status bfs_multi_run(bfs_multi *m, const uint32_t *roots, int32_t block, int
 bfs_status bfs_multi_autotune(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
                               int32_t reps, const char *cache_path, int32_t *best_block,
                               int32_t *best_ipt, float *times_ms);
+/* bfs_multi_run with cluster > 1: the batch's largest graphs (edge count at
+ * least `cluster` blocks' fair share of the batch) are each run by a cluster
+ * of `cluster` thread blocks (tiles of the frontier dealt over the cluster,
+ * claims on a per-cluster bitmap in L2, the cluster barrier as the level
+ * barrier); the other graphs run one per block as above.  Configurations:
+ * cluster 1 with block 128/256/512 and ipt 1/2/4; cluster 2/4/8 with block
+ * 256/512 and ipt 2/4.  No counterpart in the reference. */
+bfs_status bfs_multi_run_ex(bfs_multi *m, const uint32_t *roots, int32_t block, int32_t ipt,
+                            int32_t cluster, int32_t *levels_dev, uint64_t *edges_count_out,
+                            double *device_ms);
+/* bfs_multi_autotune over every configuration, clusters included; times_ms
+ * (optional) receives bfs_multi_num_configs() timings in that order. */
+bfs_status bfs_multi_autotune_ex(bfs_multi *m, const uint32_t *roots, int32_t *levels_dev,
+                                 int32_t reps, const char *cache_path, int32_t *best_block,
+                                 int32_t *best_ipt, int32_t *best_cluster, float *times_ms);
+/* The configurations of bfs_multi_autotune_ex (up to max of them into the
+ * optional arrays); returns their number. */
+int32_t bfs_multi_num_configs(int32_t *blocks, int32_t *ipts, int32_t *clusters, int32_t max);
 
 /* ---- BFS without device allocation ------------------------------------ */
 /* No counterpart in the reference (its GPURun allocates per run).  For

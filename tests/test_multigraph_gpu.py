@@ -42,13 +42,45 @@ def test_config5b_256_uneven_rmat_graphs_every_config(B, O, tmp_path):
         ec, ms = mb.run(roots, out.data_ptr(), blk, ipt)
         assert ms > 0
         check(mb, graphs, refs, out, ec)
+    # the largest graphs shared by clusters of 2 / 4 / 8 blocks
+    for blk, ipt, cl in B.MULTI_CONFIGS_ALL[len(B.MULTI_CONFIGS):]:
+        out.fill_(7)
+        ec, ms = mb.run(roots, out.data_ptr(), blk, ipt, cl)
+        check(mb, graphs, refs, out, ec)
     cache = str(tmp_path / "autotune.tsv")
-    best, times = mb.autotune(roots, out.data_ptr(), reps=2, cache_path=cache)
+    best, times = mb.autotune(roots, out.data_ptr(), reps=2, cache_path=cache, clusters=False)
     assert best in B.MULTI_CONFIGS and all(t > 0 for t in times)
-    best2, times2 = mb.autotune(roots, out.data_ptr(), cache_path=cache)
+    best2, times2 = mb.autotune(roots, out.data_ptr(), cache_path=cache, clusters=False)
     assert best2 == best and all(t == -1 for t in times2)  # served from the cache
     ec, _ = mb.run(roots, out.data_ptr(), *best)
     check(mb, graphs, refs, out, ec)
+    best3, times3 = mb.autotune(roots, out.data_ptr(), reps=2, cache_path=cache)
+    assert best3 in B.MULTI_CONFIGS_ALL and len(times3) == len(B.MULTI_CONFIGS_ALL)
+    ec, _ = mb.run(roots, out.data_ptr(), *best3)
+    check(mb, graphs, refs, out, ec)
+    mb.free()
+
+
+def test_clusters_on_deep_and_degenerate_graphs(B, O):
+    """Clustered runs on a batch whose large members are deep (grids), have
+    rows < cols, or start from a root without out-edges."""
+    torch = torch_cuda()
+    g1 = B.gen_grid(200, 150, 0.05, 4)                     # hundreds of levels
+    g2 = B.gen_rmat(13, 16, seed=5)
+    g3 = B.Csc(g2.indptr, g2.inds, g2.n_cols - 100, g2.n_cols)
+    small = [B.gen_rmat(8, 8, seed=s) for s in range(6)]
+    graphs = [g1, g2, g3] + small
+    zero_deg = int(np.flatnonzero(g2.degree() == 0)[0])
+    roots = np.array([0, zero_deg, int(B.sample_roots(g3, 1, 3)[0])] +
+                     [int(B.sample_roots(g, 1, 4)[0]) for g in small], np.uint32)
+    refs = oracle_all(O, graphs, roots)
+    mb = B.MultiBatch(graphs)
+    out = torch.empty(mb.total_cols, dtype=torch.int32, device="cuda")
+    for blk, ipt, cl in ((256, 2, 2), (512, 4, 4), (256, 4, 8), (512, 2, 8)):
+        for _ in range(2):  # the second call reuses the captured launch
+            out.fill_(7)
+            ec, _ = mb.run(roots, out.data_ptr(), blk, ipt, cl)
+            check(mb, graphs, refs, out, ec)
     mb.free()
 
 

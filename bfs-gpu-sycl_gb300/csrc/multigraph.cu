@@ -71,8 +71,9 @@ struct MultiArgs {
 // visited bitmap -- the block's own shared bitmap, or, for a graph shared by
 // a cluster (CL), the cluster's bitmap in global memory, with the shared
 // bitmap kept as a filter of already visited vertices.  The claiming thread
-// writes the level; kept vertices are appended to qn with one atomic per warp
-// round on *ctr.  Returns (in thread 0) the sum of the tiles' degrees.
+// writes the level; kept vertices are appended to qn through *ctr (a shared
+// counter per vertex, or for CL a global counter per warp round).  Returns
+// (in thread 0) the sum of the tiles' degrees.
 template <int B, int IPT, bool CL>
 __device__ __forceinline__ unsigned long long multi_level(
     const uint32_t *__restrict__ ip, const uint32_t *__restrict__ ix, int32_t *lv,
@@ -150,16 +151,20 @@ __device__ __forceinline__ unsigned long long multi_level(
               if (!(old & bit)) {
                 lv[v] = lvl + 1;
                 push = v < n_rows && ip[v + 1] > ip[v];
+                // a block's own queue: one shared-memory atomic per vertex
+                if (!CL && push) qn[atomicAdd(ctr, 1u)] = v;
               }
             }
           }
-          const uint32_t pm = __ballot_sync(kFull, push);
-          if (pm) {
-            const uint32_t leader = __ffs(pm) - 1u;
-            uint32_t base0 = 0;
-            if (lane == leader) base0 = atomicAdd(ctr, (uint32_t)__popc(pm));
-            base0 = __shfl_sync(kFull, base0, leader);
-            if (push) qn[base0 + __popc(pm & lt_mask)] = v;
+          if (CL) {  // a cluster's queue in global memory: one atomic per warp round
+            const uint32_t pm = __ballot_sync(kFull, push);
+            if (pm) {
+              const uint32_t leader = __ffs(pm) - 1u;
+              uint32_t base0 = 0;
+              if (lane == leader) base0 = atomicAdd(ctr, (uint32_t)__popc(pm));
+              base0 = __shfl_sync(kFull, base0, leader);
+              if (push) qn[base0 + __popc(pm & lt_mask)] = v;
+            }
           }
         }
       }

@@ -12,9 +12,10 @@ sees a known sequence of launches:
                   entries, edges) per level.
   batch SCALE     R-MAT SCALE/EF16 seed 6, one 64-root multi-source pass
                   (host-driven level loop, as above).
-  multi           the 256-graph mixed batch of the benchmark, one launch of
-                  the persistent multi-graph kernel (512 threads, 4 items per
-                  lane).
+  multi [B I C]   the 256-graph mixed batch of the benchmark, one launch of
+                  the persistent multi-graph kernel: B threads per block, I
+                  items per lane, clusters of C blocks for the largest graphs
+                  (default 512 4 1).
 
 Examples:
   python bfs-gpu-sycl_gb300/profile_case.py bfs 24 glb256
@@ -50,11 +51,11 @@ def case_batch(scale):
           "edges", int(ec.sum()))
 
 
-def case_multi():
+def case_multi(block=512, ipt=4, cluster=1):
     graphs, roots = B.multi_batch_graphs(B.multi_batch_specs())
     mb = B.MultiBatch(graphs)
     out = torch.empty(mb.total_cols, dtype=torch.int32, device="cuda")
-    ec, ms = mb.run(roots, out.data_ptr(), 512, 4)
+    ec, ms = mb.run(roots, out.data_ptr(), block, ipt, cluster)
     print("ms", ms, "edges", int(ec.sum()), "vertices", mb.total_cols)
 
 
@@ -67,8 +68,8 @@ def main(argv):
         case_bfs(int(argv[1]), argv[2])
     elif argv[0] == "batch" and len(argv) == 2:
         case_batch(int(argv[1]))
-    elif argv[0] == "multi" and len(argv) == 1:
-        case_multi()
+    elif argv[0] == "multi" and len(argv) in (1, 4):
+        case_multi(*(int(x) for x in argv[1:]))
     else:
         print(__doc__)
         return 2

@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(B) multi_bfs_kernel(MultiArgs a) {
 // own.  Each frontier entry is expanded by exactly one block, so the edge
 // counts stay exact.
 template <int B, int IPT, int C>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(B)
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(B, 2048 / B)
     multi_bfs_cluster_kernel(MultiArgs a) {
   extern __shared__ uint32_t s_bitmap[];
   __shared__ uint32_t s_off[B + 1];

@@ -115,9 +115,17 @@ __device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w,
 }
 
 // Copies the model to shared memory with all threads of the block: one
-// round of parallel loads instead of the MLP's dependent ones.
+// round of parallel loads instead of the MLP's dependent ones.  The loads
+// mark the model evict-last in L2, so that it stays there while each level's
+// edge stream (evict-first) passes through.
 __device__ __forceinline__ void stage_weights(float *dst, const float *__restrict__ w) {
-  for (uint32_t i = threadIdx.x; i < (uint32_t)kSchedParams; i += blockDim.x) dst[i] = w[i];
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  for (uint32_t i = threadIdx.x; i < (uint32_t)kSchedParams; i += blockDim.x) {
+    float x;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(w + i), "l"(pol));
+    dst[i] = x;
+  }
 }
 
 __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_cond) {
@@ -684,22 +692,18 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   __syncthreads();
   if (s_last) {  // uniform over the block
     // fused scheduler: the arm of the level just generated, for the
-    // explore_any launch of the next loop iteration; the model goes to the
-    // (now unused) vertex-list buffer first
+    // explore_any launch of the next loop iteration.  The block copies the
+    // model into the (now unused) vertex-list buffer while thread 0 closes
+    // the level.
     const float *w = st->sched_w;
     float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
-    if (w != nullptr) {
-      stage_weights(s_w, w);
-      __syncthreads();
+    if (w != nullptr) stage_weights(s_w, w);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      finish_level(st, cond, use_cond);
     }
-    if (warp == 0) {
-      if (lane == 0) {
-        __threadfence();
-        finish_level(st, cond, use_cond);
-      }
-      __syncwarp();
-      if (w != nullptr) fused_sched_pick(st, s_w, st->sched_cond, use_cond);
-    }
+    __syncthreads();
+    if (w != nullptr && warp == 0) fused_sched_pick(st, s_w, st->sched_cond, use_cond);
   }
 }
 

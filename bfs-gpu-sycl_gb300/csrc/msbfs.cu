@@ -339,17 +339,32 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
 // j is then four bit extracts, and the warp stores root j's 32 entries as one
 // 128-byte segment.  The root loop is unrolled so that every shift is a
 // constant.
+// Spreads the 4 low bits of n (n < 16) to bit 0 of the 4 bytes: the shifted
+// copies n, n << 7, n << 14, n << 21 do not overlap, so the product has no
+// carries and byte i holds bit i of n.
+__device__ __forceinline__ uint32_t nibble_to_bytes(uint32_t n) {
+  return (n * 0x00204081u) & 0x01010101u;
+}
+
 template <int H>
 __device__ __forceinline__ void ms_store_rows(int32_t *__restrict__ row, size_t n, uint32_t v,
                                               bool in, uint32_t nl, uint32_t r, uint32_t b0,
                                               uint32_t b1, uint32_t b2, uint32_t b3) {
+  // four roots at a time: their levels as four bytes (0xFF = unreached)
 #pragma unroll
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < 32; j += 4) {
     if ((uint32_t)(H * 32 + j) >= nl) break;  // uniform
-    const int32_t x = (int32_t)(((b0 >> j) & 1u) | (((b1 >> j) & 1u) << 1) |
-                                (((b2 >> j) & 1u) << 2) | (((b3 >> j) & 1u) << 3));
-    if (in) row[v] = ((r >> j) & 1u) ? x : -1;
-    row += n;
+    const uint32_t lv4 = nibble_to_bytes((b0 >> j) & 15u) | (nibble_to_bytes((b1 >> j) & 15u) << 1) |
+                         (nibble_to_bytes((b2 >> j) & 15u) << 2) |
+                         (nibble_to_bytes((b3 >> j) & 15u) << 3);
+    const uint32_t seen = nibble_to_bytes((r >> j) & 15u) * 0xFFu;
+    const uint32_t packed = lv4 | ~seen;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if ((uint32_t)(H * 32 + j + i) >= nl) break;  // uniform
+      if (in) row[v] = (int32_t)(int8_t)(packed >> (8 * i));
+      row += n;
+    }
   }
 }
 

@@ -237,7 +237,7 @@ __device__ __forceinline__ void multi_small_graphs(const MultiArgs &a, uint32_t 
 }
 
 template <int B, int IPT>
-__global__ void __launch_bounds__(B) multi_bfs_kernel(MultiArgs a) {
+__global__ void __launch_bounds__(B, 2048 / B) multi_bfs_kernel(MultiArgs a) {
   extern __shared__ uint32_t s_bitmap[];
   __shared__ uint32_t s_off[B + 1];
   __shared__ uint32_t s_beg[B];

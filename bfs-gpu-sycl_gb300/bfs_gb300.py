@@ -139,6 +139,8 @@ def lib():
     _sig(L, "bfs_sched_attach", [VP, C.POINTER(C.c_float), C.c_float])
     _sig(L, "bfs_run_batch", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
                               C.POINTER(BatchStats)])
+    _sig(L, "bfs_run_batch_host", [VP, U32P, C.c_uint32, I32P, C.POINTER(C.c_uint64),
+                                   C.POINTER(BatchStats)])
     _sig(L, "bfs_run_batch_loop", [VP, U32P, C.c_uint32, VP, C.POINTER(C.c_uint64),
                                    C.c_int32, C.POINTER(BatchStats)])
     _sig(L, "bfs_multi_create", [C.c_uint32, C.POINTER(U32P), C.POINTER(U32P), U32P, U32P,
@@ -496,6 +498,18 @@ class Graph:
                                        else None,
                                        LOOP_GRAPH if loop == "graph" else LOOP_HOST, C.byref(st)))
         return ec, st
+
+    def run_batch_host(self, roots, want_levels=True):
+        """Multi-source BFS into host arrays: (levels int32[len(roots), n_cols]
+        or None, edges uint64[len(roots)], BatchStats)."""
+        rt = np.ascontiguousarray(roots, np.uint32)
+        lv = np.empty((len(rt), self.n_cols), np.int32) if want_levels else None
+        ec = np.zeros(len(rt), np.uint64)
+        st = BatchStats()
+        check(lib().bfs_run_batch_host(self.h, rt.ctypes.data_as(U32P), len(rt),
+                                       lv.ctypes.data_as(I32P) if want_levels else None,
+                                       ec.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(st)))
+        return lv, ec, st
 
     def sched_record(self, root, ipt=4, reps=3, max_levels=1 << 16):
         """Per-level features and explore times of all 9 arms for one BFS."""

@@ -462,6 +462,7 @@ struct MsWorkspace {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int grid_ex = 0, grid_lg = 0, grid_xp = 0;
+  int32_t *rows = nullptr;  // one pass of level rows for bfs_run_batch_host
   size_t clear_bytes = 0;  // visited and next masks, history level 0
 };
 
@@ -476,6 +477,7 @@ void free_msbfs(bfs_graph *g) {
   if (w->e1) cudaEventDestroy(w->e1);
   cudaFree(w->mem);
   cudaFree(w->d_st);
+  cudaFree(w->rows);
   if (w->h_st) cudaFreeHost(w->h_st);
   delete w;
   g->ms = nullptr;
@@ -675,5 +677,39 @@ extern "C" bfs_status bfs_run_batch_loop(bfs_graph *g, const uint32_t *roots, ui
     }
   }
   if (stats) stats->device_ms = total_ms;
+  return BFS_OK;
+}
+
+extern "C" bfs_status bfs_run_batch_host(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                                         int32_t *levels_host, uint64_t *edges_count_out,
+                                         bfs_batch_stats *stats) {
+  if (!g || !roots) return fail(BFS_ERR_INVALID_ARG, "null pointer");
+  MK(cudaSetDevice(g->device));
+  bfs_status rc = ms_setup(g);
+  if (rc != BFS_OK) {
+    free_msbfs(g);
+    return rc;
+  }
+  MsWorkspace *w = g->ms;
+  const size_t n = g->n_cols;
+  if (!w->rows) MK(cudaMalloc(&w->rows, sizeof(int32_t) * n * kLanes));
+  bfs_batch_stats total;
+  std::memset(&total, 0, sizeof(total));
+  for (uint32_t b0 = 0; b0 < n_roots; b0 += kLanes) {
+    const uint32_t nl = std::min<uint32_t>(kLanes, n_roots - b0);
+    bfs_batch_stats st;
+    rc = bfs_run_batch_loop(g, roots + b0, nl, w->rows,
+                            edges_count_out ? edges_count_out + b0 : nullptr, BFS_LOOP_GRAPH,
+                            &st);
+    if (rc != BFS_OK) return rc;
+    total.device_ms += st.device_ms;
+    total.batches += st.batches;
+    total.max_levels = std::max(total.max_levels, st.max_levels);
+    total.launches += st.launches;
+    if (levels_host)
+      MK(cudaMemcpy(levels_host + (size_t)b0 * n, w->rows, sizeof(int32_t) * n * nl,
+                    cudaMemcpyDeviceToHost));
+  }
+  if (stats) *stats = total;
   return BFS_OK;
 }

@@ -169,6 +169,13 @@ typedef struct bfs_batch_stats {
 bfs_status bfs_run_batch(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
                          int32_t *levels_dev, uint64_t *edges_count_out,
                          bfs_batch_stats *stats);
+/* bfs_run_batch for host callers: the level rows of each pass of 64 roots go
+ * to a device buffer held by the graph handle and are copied to levels_host
+ * (n_roots x n_cols int32, optional: NULL keeps only the edge counts and
+ * stats); stats->device_ms covers the passes, not the copies. */
+bfs_status bfs_run_batch_host(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                              int32_t *levels_host, uint64_t *edges_count_out,
+                              bfs_batch_stats *stats);
 /* bfs_run_batch with the level loop chosen by loop (bfs_loop): BFS_LOOP_HOST
  * launches every kernel separately (for profilers), BFS_LOOP_GRAPH is
  * bfs_run_batch.  Same results either way. */

@@ -13,6 +13,9 @@
 // src/CMakeLists.txt:6-12):
 //   --partitions P   dataset partition count (the reference's NUM_GPU); the
 //                    partitions are merged and run on one GPU
+//   --batch K        also run the root and K - 1 seeded roots as batched
+//                    (64-root) BFS passes; adds batchRoots / batchMs /
+//                    batchRootsPerSec / batchMaxLevels / batchValid
 //   --lb llb|glb|slb|learned   explore form (default llb, or the build macro)
 //   --block 128|256|512  --ipt 4|8  --loop graph|host
 //   --weights FILE   scheduler weights for --lb learned
@@ -120,15 +123,17 @@ int main(int argc, char **argv) {
   parser.add("loop", "graph");
   parser.add("weights", exe_dir() + "/../sched_weights.f32");
   parser.add("dataset_dir", "");
+  parser.add("batch", "0");
   parser.parse(argc, argv);
 
-  int num_runs, start_vertex, parts, block, ipt;
+  int num_runs, start_vertex, parts, block, ipt, batch;
   try {
     num_runs = std::stoi(parser.get("num_runs"));
     start_vertex = std::stoi(parser.get("root"));
     parts = std::stoi(parser.get("partitions"));
     block = std::stoi(parser.get("block"));
     ipt = std::stoi(parser.get("ipt"));
+    batch = std::stoi(parser.get("batch"));
   } catch (const std::exception &e) {
     std::cerr << "ERROR: bad numeric argument (" << e.what() << ")" << std::endl;
     return 1;
@@ -136,8 +141,8 @@ int main(int argc, char **argv) {
   const std::string dataset = parser.get("dataset");
   const std::string output = parser.get("output");
   const int lb = lb_from_name(parser.get("lb"));
-  if (lb < -1 || num_runs < 1 || parts < 1 || start_vertex < 0) {
-    std::cerr << "ERROR: invalid --lb, --num_runs, --partitions or --root" << std::endl;
+  if (lb < -1 || num_runs < 1 || parts < 1 || start_vertex < 0 || batch < 0) {
+    std::cerr << "ERROR: invalid --lb, --num_runs, --partitions, --root or --batch" << std::endl;
     return 1;
   }
   parser.print();
@@ -208,6 +213,52 @@ int main(int argc, char **argv) {
             << " runs) cross checked\n";
   std::cout << "----------------------------------------" << std::endl;
 
+  // --batch K: the root and K - 1 seeded roots in passes of 64 (multi-source
+  // BFS); the root's row and edge count must equal the single-root result
+  bool batch_ok = true;
+  bfs::Json batch_obj = bfs::Json::object();
+  if (batch > 0) {
+    std::vector<uint32_t> roots(1, (uint32_t)start_vertex);
+    if (batch > 1) {
+      std::vector<uint32_t> more((size_t)batch - 1);
+      if (bfs_sample_roots(indptr.data(), numRows, (uint32_t)batch - 1, 1, more.data()) != BFS_OK) {
+        std::cerr << "ERROR: " << bfs_last_error() << std::endl;
+        return 1;
+      }
+      roots.insert(roots.end(), more.begin(), more.end());
+    }
+    bfs_graph *bg = nullptr;
+    if (bfs_graph_upload(indptr.data(), inds.data(), numRows, numCols, inds.size(), 0, &bg) !=
+        BFS_OK) {
+      std::cerr << "ERROR: " << bfs_last_error() << std::endl;
+      return 1;
+    }
+    // keep at most 1 GiB of rows on the host; beyond that only the counts
+    const bool keep = (double)batch * numCols * 4.0 <= 1073741824.0;
+    std::vector<int32_t> rows(keep ? (size_t)batch * numCols : 0);
+    std::vector<uint64_t> bedges((size_t)batch);
+    bfs_batch_stats bst;
+    const bfs_status bs = bfs_run_batch_host(bg, roots.data(), (uint32_t)batch,
+                                             keep ? rows.data() : nullptr, bedges.data(), &bst);
+    bfs_graph_free(bg);
+    if (bs != BFS_OK) {
+      std::cerr << "ERROR: " << bfs_last_error() << std::endl;
+      return 1;
+    }
+    batch_ok = bedges[0] == cfg.edges_count;
+    if (keep)
+      for (uint32_t v = 0; v < numCols && batch_ok; v++)
+        batch_ok = rows[v] == h_distancesGPU.back()[v];
+    batch_obj["batchRoots"] = batch;
+    batch_obj["batchMs"] = bst.device_ms;
+    batch_obj["batchRootsPerSec"] = bst.device_ms > 0 ? 1e3 * batch / bst.device_ms : 0.0;
+    batch_obj["batchMaxLevels"] = (long long)bst.max_levels;
+    batch_obj["batchValid"] = batch_ok;
+    std::cout << "- batch: " << batch << " roots in " << bst.batches << " passes, "
+              << bst.device_ms << " ms, root row " << (batch_ok ? "agrees" : "DIFFERS")
+              << std::endl;
+  }
+
   const double edges = (double)cfg.edges_count;
   const double avg_ms = obj["avgExecutionTime"].as_double();
   const double avg90 = obj["avgExecutionTime90f"].as_double();
@@ -235,6 +286,9 @@ int main(int argc, char **argv) {
   obj["variant"] = variant_key(lb < 0 ? bfs::default_lb() : lb);
   obj["blockSize"] = block;
   obj["validationErrors"] = (unsigned long long)cfg.validation_errors;
+  for (const char *k : {"batchRoots", "batchMs", "batchRootsPerSec", "batchMaxLevels",
+                        "batchValid"})
+    if (batch > 0) obj[k] = batch_obj[k];
 
   bfs::Json combined = bfs::Json::object();
   {
@@ -260,5 +314,5 @@ int main(int argc, char **argv) {
     return 1;
   }
   out << combined.dump(4);
-  return status ? 0 : 2;
+  return status && batch_ok ? 0 : 2;
 }

@@ -89,3 +89,23 @@ def test_cli_partitions_and_merge(B, O, tmp_path):
     for P in ("1", "3"):
         obj = rep["mp_1_global"][P]
         assert obj["edgesCount"] == ec and obj["valid"] is True
+
+
+@pytest.mark.gpu
+def test_cli_batch_option(B, O, tmp_path):
+    """--batch K runs the root and K - 1 seeded roots as 64-root passes; the
+    root's row and edge count agree with the single-root runs."""
+    g = B.gen_rmat(13, 16, seed=22)
+    B.dataset_write(g, "rb", 1, str(tmp_path / "dataset"))
+    root = int(B.sample_roots(g, 1, 22)[0])
+    r = run_cli(["--dataset=rb", f"--root={root}", "--num_runs=2", "--lb=glb", "--batch=70"],
+                tmp_path)
+    assert r.returncode == 0, r.stderr
+    obj = json.load(open(tmp_path / "data.json"))["rb_2_global"]["1"]
+    lv, ec = O.oracle_bfs(g.indptr, g.inds, root)
+    assert obj["batchRoots"] == 70 and obj["batchValid"] is True
+    assert obj["batchMs"] > 0 and obj["batchRootsPerSec"] > 0
+    assert obj["batchMaxLevels"] >= int(lv.max()) + 1
+    assert obj["edgesCount"] == ec
+    r = run_cli(["--dataset=rb", f"--root={root}", "--batch=-1"], tmp_path)
+    assert r.returncode == 1

@@ -107,3 +107,22 @@ def test_history_boundary_depths(B, O):
             assert np.array_equal(ec, rec), (n, loop)
             assert st.max_levels == int(ref.max()) + 1
         dg.free()
+
+
+def test_batch_into_host_arrays(B, O):
+    """bfs_run_batch_host: rows copied to host per pass, equal to the device
+    entry point's rows and to the oracle."""
+    torch = torch_cuda()
+    g = B.gen_rmat(14, 8, seed=31)
+    dg = B.Graph.upload(g)
+    roots = B.sample_roots(g, 80, 31)
+    lv, ec, st = dg.run_batch_host(roots)
+    assert st.batches == 2 and st.device_ms > 0
+    ref, rec = O.oracle_bfs_many(g.indptr, g.inds, roots)
+    assert np.array_equal(lv, ref) and np.array_equal(ec, rec)
+    none, ec2, _ = dg.run_batch_host(roots, want_levels=False)
+    assert none is None and np.array_equal(ec2, rec)
+    out = torch.empty((len(roots), g.n_cols), dtype=torch.int32, device="cuda")
+    ec3, _ = dg.run_batch(roots, out.data_ptr())
+    assert np.array_equal(out.cpu().numpy(), lv) and np.array_equal(ec3, ec)
+    dg.free()

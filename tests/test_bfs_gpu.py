@@ -266,3 +266,31 @@ def test_rmat25_full_size(B, O):
                 first = cur
             assert np.array_equal(cur, first)
     dg.free()
+
+
+def test_pinned_host_outputs(B, O):
+    """bfs_run into pinned host buffers and into pageable ones: same levels
+    and parents, twice; and into a pinned buffer at an odd offset."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    g = B.gen_rmat(15, 16, seed=41)
+    dg = B.Graph.upload(g)
+    n = g.n_cols
+    for r in B.sample_roots(g, 2, 41):
+        ref, ec = O.oracle_bfs(g.indptr, g.inds, int(r))
+        for rep in range(2):
+            lv_p = torch.full((n,), 7, dtype=torch.int32, pin_memory=True)
+            pa_p = torch.full((n,), 7, dtype=torch.int32, pin_memory=True)
+            st = dg.run_into(int(r), lv_p.data_ptr(), pa_p.data_ptr())
+            assert np.array_equal(lv_p.numpy(), ref) and st.edges_count == ec
+            lv, pa, _ = dg.run(int(r), parents=True)
+            assert np.array_equal(lv, ref)
+            pp = pa_p.numpy()
+            kids = np.flatnonzero(ref > 0)
+            assert np.all(ref[pp[kids]] == ref[kids] - 1) and pp[int(r)] == int(r)
+        # an odd-sized tail: a pinned buffer offset by one element
+        big = torch.full((n + 1,), 7, dtype=torch.int32, pin_memory=True)
+        dg.run_into(int(r), big.data_ptr() + 4)
+        assert np.array_equal(big.numpy()[1:], ref) and big[0].item() == 7
+    dg.free()

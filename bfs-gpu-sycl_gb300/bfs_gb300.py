@@ -113,6 +113,8 @@ def lib():
     _sig(L, "bfs_graph_device_csc", [VP, C.POINTER(VP), C.POINTER(VP)])
     _sig(L, "bfs_run", [VP, C.c_uint32, C.POINTER(Options), I32P, I32P, C.POINTER(Stats)])
     _sig(L, "bfs_run_device", [VP, C.c_uint32, C.POINTER(Options), VP, VP, C.POINTER(Stats)])
+    _sig(L, "bfs_run_roots", [VP, U32P, C.c_uint32, C.POINTER(Options), C.POINTER(VP),
+                              C.POINTER(VP), C.POINTER(Stats)])
     _sig(L, "bfs_validate_device", [VP, C.c_uint32, VP, VP, C.POINTER(C.c_uint64)])
     _sig(L, "bfs_csc_host_free", [C.POINTER(CscHost)], None)
     _sig(L, "bfs_gen_rmat_host", [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
@@ -476,6 +478,22 @@ class Graph:
                             C.cast(parents_host_ptr, I32P) if parents_host_ptr else None,
                             C.byref(st) if st is not None else None))
         return st
+
+    def run_roots(self, roots, levels_host_ptrs, parents_host_ptrs=None, opts=None):
+        """One BFS per root in one call (bfs_run_roots): run i writes host
+        buffer levels_host_ptrs[i] (and parents_host_ptrs[i]); returns the
+        runs' Stats.  With pinned buffers run i's copy overlaps run i + 1."""
+        r = np.ascontiguousarray(roots, np.uint32)
+        k = len(r)
+        if len(levels_host_ptrs) != k or (parents_host_ptrs is not None
+                                          and len(parents_host_ptrs) != k):
+            raise ValueError("one output buffer per root")
+        lp = (VP * max(k, 1))(*[VP(p) for p in levels_host_ptrs])
+        pp = (VP * max(k, 1))(*[VP(p) for p in parents_host_ptrs]) if parents_host_ptrs else None
+        st = (Stats * max(k, 1))()
+        check(lib().bfs_run_roots(self.h, r.ctypes.data_as(U32P), k,
+                                  C.byref(opts) if opts is not None else None, lp, pp, st))
+        return list(st)[:k]
 
     def run_device(self, root, levels_ptr, parents_ptr=None, opts=None, stats=True):
         st = Stats() if stats else None

@@ -69,6 +69,19 @@ static void free_workspace(bfs_graph *g) {
   cudaFree(g->d_out_levels);
   cudaFree(g->d_out_parents);
   g->d_out_levels = g->d_out_parents = nullptr;
+  for (auto &slot : g->d_ring)
+    for (auto &p : slot) {
+      cudaFree(p);
+      p = nullptr;
+    }
+  if (g->ev_ready) cudaEventDestroy(g->ev_ready);
+  g->ev_ready = nullptr;
+  for (auto &e : g->ev_copied) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
+  g->copy_stream = nullptr;
   if (g->h_st) cudaFreeHost(g->h_st);
   g->h_st = nullptr;
   if (g->ev0) cudaEventDestroy(g->ev0);
@@ -334,18 +347,9 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   int one = 1;
   BfsDevState *st = g->d_st;
 
-  cudaGraphNode_t n_memset, n_fill, n_init, n_while, n_explore, n_lg;
-  cudaMemsetParams mp;
-  std::memset(&mp, 0, sizeof(mp));
-  mp.dst = g->ws;
-  mp.value = 0;
-  mp.elementSize = 4;
-  mp.width = g->bitmap_bytes / 4;
-  mp.height = 1;
-  mp.pitch = 0;
-  CK(cudaGraphAddMemsetNode(&n_memset, graph, nullptr, 0, &mp));
-  void *fill_args[] = {&st};
-  CK(add_kernel(graph, &n_fill, &n_memset, 1, fill_kernel_fn(), g->num_sms * 4, 256, fill_args));
+  cudaGraphNode_t n_fill, n_init, n_while, n_explore, n_lg;
+  void *fill_args[] = {&st};  // levels (and parents) to -1, bitmaps cleared
+  CK(add_kernel(graph, &n_fill, nullptr, 0, fill_kernel_fn(), g->num_sms * 4, 256, fill_args));
   void *init_args[] = {&st, &cond_arg, &one};
   CK(add_kernel(graph, &n_init, &n_fill, 1, init_kernel_fn(), 1, 32, init_args));
 
@@ -426,7 +430,6 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, int ipt,
   const bool prof = g->prof_explore != nullptr;
   const bool learned = arm_fixed < 0;
   void *fill_args[] = {&st};
-  CK(cudaMemsetAsync(g->ws, 0, g->bitmap_bytes, g->stream));
   CK(cudaLaunchKernel(fill_kernel_fn(), dim3(g->num_sms * 4), dim3(256), fill_args, 0, g->stream));
   void *init_args[] = {&st, &no_cond, &zero};
   CK(cudaLaunchKernel(init_kernel_fn(), dim3(1), dim3(32), init_args, 0, g->stream));
@@ -466,7 +469,7 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, int ipt,
 
 bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_in,
                            int32_t *levels_dev, int32_t *parents_dev, bfs_stats *stats,
-                           LevelTimer *timer) {
+                           LevelTimer *timer, const std::function<bfs_status()> *after_launch) {
   if (!g || !levels_dev) return fail(BFS_ERR_INVALID_ARG, "null graph or level buffer");
   if (root >= g->n_cols) return fail(BFS_ERR_ROOT, "root out of range");
   bfs_options o;
@@ -525,7 +528,7 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     }
   }
   CK(cudaEventRecord(g->ev0, g->stream));
-  CK(cudaMemcpyAsync(g->d_st, g->h_st, sizeof(BfsDevState), cudaMemcpyHostToDevice, g->stream));
+  CK(launch_seed_state(g->d_st, *g->h_st, g->stream));
   uint32_t launches = 0;
   if (graph_loop) {
     CK(cudaGraphLaunch(ge->exec, g->stream));
@@ -535,6 +538,13 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     launches = g->host_launches;
   }
   CK(cudaEventRecord(g->ev1, g->stream));
+  if (after_launch) {
+    rc = (*after_launch)();
+    if (rc != BFS_OK) {
+      cudaStreamSynchronize(g->stream);
+      return rc;
+    }
+  }
   rc = read_state(g);
   if (rc != BFS_OK) return rc;
   const BfsDevState &r = *g->h_st;
@@ -548,7 +558,7 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     stats->reached = r.reached;
     stats->num_levels = r.max_level + 1;
     stats->device_ms = ms;
-    stats->launches = launches ? launches : r.launches + 1;  // + memset node
+    stats->launches = (launches ? launches : r.launches) + 1;  // + the seed kernel
     stats->recorded = 0;
     if (o.record < 2) {
       std::memset(stats->level_explore_ms, 0, sizeof(stats->level_explore_ms));
@@ -720,6 +730,73 @@ bfs_status bfs_run(bfs_graph *g, uint32_t root, const bfs_options *opts, int32_t
     CK(cudaMemcpyAsync(parents_host, g->d_out_parents, bytes, cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
   return BFS_OK;
+}
+
+// Runs i and i + 1 write device buffers of alternating slots; run i's copy
+// to the host is queued on the copy stream once run i + 1 is queued, so it
+// overlaps run i + 1, and run i + 2 waits on the main stream for that copy
+// before it overwrites the slot.  Device-to-host copies into pageable memory
+// return only when done, so with pageable buffers the runs are serial.
+static bfs_status run_roots_impl(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                                 const bfs_options *opts, int32_t *const *levels_host,
+                                 int32_t *const *parents_host, bfs_stats *stats) {
+  const size_t bytes = sizeof(int32_t) * (size_t)g->n_cols;
+  const int kinds = parents_host ? 2 : 1;
+  for (int slot = 0; slot < (n_roots > 1 ? 2 : 1); slot++)
+    for (int k = 0; k < kinds; k++)
+      if (!g->d_ring[slot][k]) CK(cudaMalloc(&g->d_ring[slot][k], bytes));
+  if (!g->copy_stream) CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+  if (!g->ev_ready) CK(cudaEventCreateWithFlags(&g->ev_ready, cudaEventDisableTiming));
+  for (auto &e : g->ev_copied)
+    if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // queues the copy of finished run j (its device buffers are slot j & 1)
+  auto copy_out = [&](uint32_t j) -> bfs_status {
+    const int slot = (int)(j & 1u);
+    CK(cudaStreamWaitEvent(g->copy_stream, g->ev_ready, 0));
+    CK(cudaMemcpyAsync(levels_host[j], g->d_ring[slot][0], bytes, cudaMemcpyDeviceToHost,
+                       g->copy_stream));
+    if (parents_host)
+      CK(cudaMemcpyAsync(parents_host[j], g->d_ring[slot][1], bytes, cudaMemcpyDeviceToHost,
+                         g->copy_stream));
+    CK(cudaEventRecord(g->ev_copied[slot], g->copy_stream));
+    return BFS_OK;
+  };
+  for (uint32_t i = 0; i < n_roots; i++) {
+    const int slot = (int)(i & 1u);
+    if (i >= 2) CK(cudaStreamWaitEvent(g->stream, g->ev_copied[slot], 0));
+    // run i-1's copy is issued after run i is queued, so that it does not
+    // hold up the start of run i, and before the wait for run i
+    const std::function<bfs_status()> prev_copy = [&]() { return copy_out(i - 1); };
+    // returns after the run has finished (it reads the device state back)
+    bfs_status rc = run_device_impl(g, roots[i], opts, g->d_ring[slot][0],
+                                    parents_host ? g->d_ring[slot][1] : nullptr,
+                                    stats ? stats + i : nullptr, nullptr,
+                                    i > 0 ? &prev_copy : nullptr);
+    if (rc != BFS_OK) return rc;
+    CK(cudaEventRecord(g->ev_ready, g->stream));  // run i has finished
+  }
+  return copy_out(n_roots - 1);
+}
+
+bfs_status bfs_run_roots(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                         const bfs_options *opts, int32_t *const *levels_host,
+                         int32_t *const *parents_host, bfs_stats *stats) {
+  if (!g || (n_roots && (!roots || !levels_host)))
+    return fail(BFS_ERR_INVALID_ARG, "null graph, roots or level buffers");
+  for (uint32_t i = 0; i < n_roots; i++) {
+    if (!levels_host[i] || (parents_host && !parents_host[i]))
+      return fail(BFS_ERR_INVALID_ARG, "null output buffer of run " + std::to_string(i));
+    if (roots[i] >= g->n_cols) return fail(BFS_ERR_ROOT, "root out of range");
+  }
+  if (n_roots == 0) return BFS_OK;
+  CK(cudaSetDevice(g->device));
+  const bfs_status rc = run_roots_impl(g, roots, n_roots, opts, levels_host, parents_host, stats);
+  // no copy into the caller's buffers is left in flight, also after an error
+  if (g->copy_stream) {
+    const cudaError_t e = cudaStreamSynchronize(g->copy_stream);
+    if (rc == BFS_OK && e != cudaSuccess) return fail(BFS_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return rc;
 }
 
 bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *levels_dev,

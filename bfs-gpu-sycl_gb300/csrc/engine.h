@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <vector>
 
@@ -26,9 +27,13 @@ struct LevelTimer {
   void (*after)(void *ctx, bfs_graph *g, uint32_t level, int arm) = nullptr;
 };
 
+// after_launch (optional) runs once the BFS is queued on the handle's stream
+// and before the call waits for it: work issued there (e.g. copies on another
+// stream) is queued ahead of the run's final state read.
 bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts,
                            int32_t *levels_dev, int32_t *parents_dev, bfs_stats *stats,
-                           LevelTimer *timer);
+                           LevelTimer *timer,
+                           const std::function<bfs_status()> *after_launch = nullptr);
 // Launches one explore kernel on the handle's stream for a frontier of F
 // entries and EF edges; persistent = full persistent grid (as in the graph
 // loop) instead of a grid sized to the frontier.
@@ -58,7 +63,10 @@ struct bfs_graph {
   bfsgb::BfsDevState *h_st = nullptr;  // pinned mirror
   int32_t *d_out_levels = nullptr;     // scratch outputs of bfs_run
   int32_t *d_out_parents = nullptr;
+  int32_t *d_ring[2][2] = {};          // bfs_run_roots: [slot][levels, parents]
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // bfs_run_roots: device-to-host copies
+  cudaEvent_t ev_ready = nullptr, ev_copied[2] = {nullptr, nullptr};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t lvl_ev[3] = {nullptr, nullptr, nullptr};  // per-level kernel timing
   float *prof_explore = nullptr;  // host arrays filled by the host loop (record == 2)

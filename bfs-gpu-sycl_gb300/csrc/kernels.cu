@@ -86,6 +86,23 @@ __global__ void fill_kernel(BfsDevState *st) {
   }
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < st->rec_cap; i += stride)
     st->rec_ran[i] = -1;
+  // cleared bitmaps: kernel stores rather than a memset, so that a BFS uses
+  // no copy engine between its start and its final state read (words is a
+  // multiple of 32 and both bitmaps are 16-byte aligned)
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (st->words >> 2); i += stride) {
+    reinterpret_cast<uint4 *>(st->vis)[i] = zero;
+    reinterpret_cast<uint4 *>(st->prev)[i] = zero;
+  }
+}
+
+// The host template of the state, passed by value: seeding the state is a
+// kernel rather than a host-to-device copy, for the same reason.
+__global__ void seed_state_kernel(BfsDevState *st, BfsDevState s) {
+  static_assert(sizeof(BfsDevState) % 4 == 0, "state is copied in words");
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(&s);
+  uint32_t *dst = reinterpret_cast<uint32_t *>(st);
+  for (uint32_t i = threadIdx.x; i < sizeof(BfsDevState) / 4; i += blockDim.x) dst[i] = src[i];
 }
 
 // Records, for the level being explored, which explore kernel ran.
@@ -831,6 +848,11 @@ cudaError_t launch_validate(const uint32_t *indptr, const uint32_t *inds, uint32
                                              parent_ok, bad);
   validate_vertices_kernel<<<1024, 256, 0, s>>>(n_cols, root, level, parent, witness,
                                                 parent_ok, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seed_state(BfsDevState *st, const BfsDevState &s, cudaStream_t stream) {
+  seed_state_kernel<<<1, 64, 0, stream>>>(st, s);
   return cudaGetLastError();
 }
 

@@ -26,7 +26,10 @@ const void *explore_kernel_fn(int arm, int ipt, bool parents);
 const void *explore_any_kernel_fn(int ipt, bool parents);
 const void *levelgen_kernel_fn();
 const void *init_kernel_fn();
+// fill also clears the visited bitmaps (vis, prev: st->words words each).
 const void *fill_kernel_fn();
+// Writes the state st from a host copy with one small kernel.
+cudaError_t launch_seed_state(BfsDevState *st, const BfsDevState &s, cudaStream_t stream);
 
 cudaError_t launch_validate(const uint32_t *indptr, const uint32_t *inds, uint32_t n_rows,
                             uint32_t n_cols, uint32_t root, const int32_t *level,

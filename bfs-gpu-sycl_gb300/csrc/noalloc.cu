@@ -153,11 +153,9 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
   BfsDevState *st = (BfsDevState *)(base + kStateOff);
   unsigned long long *bad = (unsigned long long *)(base + kBadOff);
 
-  // state + cleared counters, cleared bitmaps, CSC check
+  // state + cleared counters, CSC check (fill clears the bitmaps)
   noalloc_state_kernel<<<1, 32, 0, s>>>(h, st, bad);
   NK(cudaGetLastError());
-  NK(cudaMemsetAsync(h.vis, 0, (size_t)h.words * 4, s));
-  NK(cudaMemsetAsync(h.prev, 0, (size_t)h.words * 4, s));
   NK(launch_check_csc(d_indptr, d_inds, n_cols, nnz, bad, s));
   unsigned long long h_bad = 0;
   NK(cudaMemcpyAsync(&h_bad, bad, sizeof(h_bad), cudaMemcpyDeviceToHost, s));

@@ -136,6 +136,17 @@ bfs_status bfs_graph_device_csc(const bfs_graph *g, const uint32_t **d_indptr,
  * of the call.  stats may be NULL.  opts may be NULL (defaults). */
 bfs_status bfs_run(bfs_graph *g, uint32_t root, const bfs_options *opts,
                    int32_t *levels_host, int32_t *parents_host, bfs_stats *stats);
+/* n_roots BFS runs in one call, one per entry of roots, into host buffers:
+ * run i writes its level array to levels_host[i] and, if parents_host is not
+ * NULL, its parent array to parents_host[i] (n_cols int32 each).  This is the
+ * reference's per-run loop (run_bfs_gpu.hpp:682-730, h_distance[i] per run).
+ * The device-to-host copy of run i overlaps run i + 1 when the buffers are
+ * pinned host memory; with pageable buffers the runs are serial.  stats, if
+ * not NULL, receives n_roots entries.  Every root is checked before the
+ * first run; on an error no copy is left in flight. */
+bfs_status bfs_run_roots(bfs_graph *g, const uint32_t *roots, uint32_t n_roots,
+                         const bfs_options *opts, int32_t *const *levels_host,
+                         int32_t *const *parents_host, bfs_stats *stats);
 /* Same, with device output buffers (levels_dev required, parents_dev
  * optional); nothing is copied to the host except the small stats. */
 bfs_status bfs_run_device(bfs_graph *g, uint32_t root, const bfs_options *opts,

@@ -114,6 +114,9 @@ void GPURun(uint32_t vertexCount, vectorT &IndexHost, vectorT &OffsetHost,
   if (num_runs < 1 || h_distance.size() < (size_t)num_runs)
     throw std::runtime_error("GPURun: h_distance must hold num_runs rows");
   const uint32_t n_cols = (uint32_t)h_distance[0].size();
+  for (int i = 1; i < num_runs; i++)
+    if (h_distance[(size_t)i].size() != (size_t)n_cols)
+      throw std::runtime_error("GPURun: h_distance rows differ in length");
   std::vector<uint32_t> ip, ix;
   const std::vector<uint32_t> *pip = nullptr, *pix = nullptr;
   if constexpr (std::is_same_v<vectorT, std::vector<uint32_t>>) {
@@ -150,12 +153,16 @@ void GPURun(uint32_t vertexCount, vectorT &IndexHost, vectorT &OffsetHost,
       check_status(bfs_sched_attach(g, w.data(), cfg.min_confidence), "bfs_sched_attach");
     }
     std::vector<double> run_times((size_t)num_runs, 0.0);
-    bfs_stats st;
-    for (int i = 0; i < num_runs; i++) {
-      check_status(bfs_run(g, (uint32_t)sourceNode, &o, h_distance[(size_t)i].data(), nullptr, &st),
-                   "bfs_run");
-      run_times[(size_t)i] = st.device_ms;
-    }
+    // the num_runs loop of run_bfs_gpu.hpp:682-730 as one bfs_run_roots call
+    const std::vector<uint32_t> roots((size_t)num_runs, (uint32_t)sourceNode);
+    std::vector<int32_t *> outs((size_t)num_runs);
+    for (int i = 0; i < num_runs; i++) outs[(size_t)i] = h_distance[(size_t)i].data();
+    std::vector<bfs_stats> stats((size_t)num_runs);
+    check_status(bfs_run_roots(g, roots.data(), (uint32_t)num_runs, &o, outs.data(), nullptr,
+                               stats.data()),
+                 "bfs_run_roots");
+    for (int i = 0; i < num_runs; i++) run_times[(size_t)i] = stats[(size_t)i].device_ms;
+    const bfs_stats &st = stats.back();
     cfg.edges_count = st.edges_count;
     cfg.num_levels = st.num_levels;
     cfg.run_ms = run_times;

@@ -294,3 +294,43 @@ def test_pinned_host_outputs(B, O):
         dg.run_into(int(r), big.data_ptr() + 4)
         assert np.array_equal(big.numpy()[1:], ref) and big[0].item() == 7
     dg.free()
+
+
+def test_run_roots_pinned_and_pageable(B, O):
+    """bfs_run_roots: several roots in one call, each run's levels (and
+    parents) in its own host buffer -- pinned (copies overlap the next run)
+    and pageable (serial) -- equal to the oracle; a bad root anywhere in the
+    list is refused before any run."""
+    torch = torch_cuda()
+    g = B.gen_rmat(14, 16, seed=43)
+    dg = B.Graph.upload(g)
+    n = g.n_cols
+    roots = [int(r) for r in B.sample_roots(g, 4, 43)]
+    roots = roots + [roots[0]]  # a root repeated, as the reference's num_runs loop does
+    refs = [O.oracle_bfs(g.indptr, g.inds, r) for r in roots]
+    w = np.random.default_rng(43).normal(0, 1.0, B.SCHED_PARAMS).astype(np.float32)
+    dg.sched_attach(w)  # random weights: arbitrary arms per level
+    for learned in (False, True):
+        opts = B.options("learned") if learned else B.options("glb", 256)
+        lv = [torch.full((n,), 7, dtype=torch.int32, pin_memory=True) for _ in roots]
+        pa = [torch.full((n,), 7, dtype=torch.int32, pin_memory=True) for _ in roots]
+        sts = dg.run_roots(roots, [t.data_ptr() for t in lv], [t.data_ptr() for t in pa], opts)
+        for r, (ref, ec), st, l, p in zip(roots, refs, sts, lv, pa):
+            assert np.array_equal(l.numpy(), ref) and st.edges_count == ec
+            pp = p.numpy()
+            kids = np.flatnonzero(ref > 0)
+            assert np.all(ref[pp[kids]] == ref[kids] - 1) and pp[r] == r
+    hv = [np.full(n, 7, np.int32) for _ in roots]
+    sts = dg.run_roots(roots, [a.ctypes.data for a in hv])
+    for (ref, ec), st, a in zip(refs, sts, hv):
+        assert np.array_equal(a, ref) and st.edges_count == ec
+    # one root; then none
+    one = np.full(n, 7, np.int32)
+    dg.run_roots(roots[1:2], [one.ctypes.data])
+    assert np.array_equal(one, refs[1][0])
+    assert dg.run_roots([], []) == []
+    bad = [np.full(n, 7, np.int32) for _ in range(3)]
+    with pytest.raises(B.BfsError):
+        dg.run_roots([roots[0], n, roots[1]], [a.ctypes.data for a in bad])
+    assert all(np.all(a == 7) for a in bad)
+    dg.free()

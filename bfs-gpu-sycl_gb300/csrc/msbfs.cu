@@ -5,9 +5,12 @@
 // roots share every level: each vertex carries a 64-bit visited mask (bit j =
 // reached by root j) and the frontier queue carries, per entry, the mask of
 // roots whose frontier contains it.  One traversal of an edge u->v serves every
-// root whose frontier holds u:  next[v] |= mask(u) & ~visited[v].
-// Level generation turns next[] into the new frontier and records, per
-// level, the mask of roots that reached each vertex; an expansion kernel
+// root whose frontier holds u:  visited[v] |= mask(u) & ~visited[v], the test
+// reading the mask as the level is being explored, so that a root already
+// given to v by another edge costs no atomic.
+// Level generation compares visited[] with its copy as of the previous level
+// (prev[]) to get the new frontier and records, per level, the mask of roots
+// that reached each vertex; an expansion kernel
 // writes each root's int32 level row once, coalesced, from those masks, and
 // each root's edgesCount (sum of degrees of the vertices that root expands,
 // run_bfs_cpu.hpp:36), so every row is exactly the single-root level array
@@ -17,7 +20,7 @@
 //             frontier's edges, finds the owner of its first edge with a 32-ary
 //             search of the degree prefix, then takes each owner's first edge
 //             and root mask from shuffles of coalesced loads.
-//   levelgen  one vertex per lane: new = next[v] & ~visited[v], stored as
+//   levelgen  one vertex per lane: new = visited[v] & ~prev[v], stored as
 //             hist[L][v] for the first kHistLevels levels (one coalesced 8-byte
 //             store per vertex; level rows written level by level would be
 //             scattered partial-sector stores, which HBM turns into
@@ -54,7 +57,7 @@ struct MsState {
   const uint32_t *inds;
   uint32_t n_rows, n_cols;
   unsigned long long *vis;
-  unsigned long long *next;
+  unsigned long long *prev;  // vis as of the previous level
   unsigned long long *hist;  // kHistLevels arrays of n_cols masks
   uint32_t *qb[2];
   uint32_t *qp[2];
@@ -76,6 +79,7 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
   if (j < st->n_lanes) {
     const uint32_t r = st->roots[j];
     atomicOr(&st->vis[r], 1ull << j);
+    atomicOr(&st->prev[r], 1ull << j);
     atomicOr(&st->hist[r], 1ull << j);  // level 0
   }
   if (j < kLanes) st->edges[j] = 0;
@@ -116,7 +120,8 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
 
 // Explore: the single-root GLB walk (one difference per entry, a 32-entry
 // window re-based only when a round could leave it) with a root mask per
-// entry: next[v] |= mask(u) & ~vis[v].
+// entry: vis[v] |= mask(u) & ~vis[v].  The plain load may see a stale mask,
+// which costs only a redundant atomic.
 __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     ms_explore_kernel(MsState *__restrict__ st) {
   constexpr int NW = kMsBlock / 32;
@@ -130,8 +135,7 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
   const uint32_t *__restrict__ qp = st->qp[cq];
   const unsigned long long *__restrict__ qm = st->qm[cq];
   const uint32_t *__restrict__ inds = st->inds;
-  const unsigned long long *vis = st->vis;
-  unsigned long long *next = st->next;
+  unsigned long long *vis = st->vis;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
   const uint32_t total_warps = gridDim.x * NW;
@@ -191,8 +195,11 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
 #pragma unroll
       for (int u = 0; u < U; u++) {
         if (nb[u] == kFull) continue;
+        // roots that reached v before this level, then roots that another
+        // edge already gave v in this level: most edges of a dense level end
+        // at one of the two tests, and the atomic runs only for new roots
         const unsigned long long bits = msk[u] & ~vis[nb[u]];
-        if (bits) atomicOr(next + nb[u], bits);
+        if (bits) atomicOr(vis + nb[u], bits);
       }
     }
   }
@@ -220,7 +227,8 @@ __device__ void ms_finish(MsState *st, unsigned long long cond, int use_cond) {
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
 }
 
-// Level generation, one vertex per thread: new = next[v] & ~vis[v].  Levels
+// Level generation, one vertex per thread: new = vis[v] & ~prev[v] (then
+// prev[v] = vis[v]).  Levels
 // below kHistLevels are recorded as masks, hist[L][v] = new (written for
 // every vertex, coalesced; ms_expand_kernel turns them into the level rows);
 // deeper levels are written straight into the rows.  Kept vertices are
@@ -235,7 +243,7 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
   __shared__ uint32_t s_any;
   const uint32_t n_cols = st->n_cols, n_rows = st->n_rows;
   unsigned long long *__restrict__ vis = st->vis;
-  unsigned long long *__restrict__ next = st->next;
+  unsigned long long *__restrict__ prev = st->prev;
   const uint32_t *__restrict__ indptr = st->indptr;
   int32_t *__restrict__ level = st->level;
   const uint32_t L = st->lvl + 1;
@@ -256,17 +264,13 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
     unsigned long long nw = 0;
     uint32_t b = 0, e = 0;
     if (v < n_cols) {
-      const unsigned long long nx = next[v];
-      if (nx) {
-        next[v] = 0;
-        const unsigned long long vv = vis[v];
-        nw = nx & ~vv;
-        if (nw) {
-          vis[v] = vv | nw;
-          if (v < n_rows) {
-            b = indptr[v];
-            e = indptr[v + 1];
-          }
+      const unsigned long long vv = vis[v];
+      nw = vv & ~prev[v];
+      if (nw) {
+        prev[v] = vv;
+        if (v < n_rows) {
+          b = indptr[v];
+          e = indptr[v + 1];
         }
       }
       if (hist) hist[v] = nw;
@@ -463,7 +467,7 @@ struct MsWorkspace {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int grid_ex = 0, grid_lg = 0, grid_xp = 0;
   int32_t *rows = nullptr;  // one pass of level rows for bfs_run_batch_host
-  size_t clear_bytes = 0;  // visited and next masks, history level 0
+  size_t clear_bytes = 0;  // visited and prev masks, history level 0
 };
 
 namespace bfsgb {
@@ -514,7 +518,7 @@ static bfs_status ms_setup(bfs_graph *g) {
   s.n_rows = g->n_rows;
   s.n_cols = g->n_cols;
   s.vis = (unsigned long long *)p; p += b64;
-  s.next = (unsigned long long *)p; p += b64;
+  s.prev = (unsigned long long *)p; p += b64;
   s.hist = (unsigned long long *)p; p += kHistLevels * b64;
   for (int b = 0; b < 2; b++) {
     s.qb[b] = (uint32_t *)p; p += q4;
@@ -522,7 +526,7 @@ static bfs_status ms_setup(bfs_graph *g) {
     s.qm[b] = (unsigned long long *)p; p += q8;
   }
   s.level_cap = g->n_cols + 1u;
-  w->clear_bytes = 3 * b64;  // vis, next, hist[0] are contiguous
+  w->clear_bytes = 3 * b64;  // vis, prev, hist[0] are contiguous
   int occ_ex = 0, occ_lg = 0, occ_xp = 0;
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, (const void *)ms_explore_kernel,
                                                    kMsBlock, 0));
@@ -534,7 +538,7 @@ static bfs_status ms_setup(bfs_graph *g) {
   w->grid_lg = g->num_sms * std::max(occ_lg, 1);
   w->grid_xp = g->num_sms * std::max(occ_xp, 1);
 
-  // graph: memset(vis, next, hist[0]) -> init ->
+  // graph: memset(vis, prev, hist[0]) -> init ->
   //   while(F > 0) { explore -> levelgen -> expand(in loop) } -> expand(final)
   MK(cudaGraphCreate(&w->graph, 0));
   cudaGraphConditionalHandle cond;

@@ -24,7 +24,7 @@ def declared_functions():
 
 def test_header_declares_entry_points():
     names = declared_functions()
-    for n in ("bfs_graph_upload", "bfs_run", "bfs_run_device", "bfs_graph_free",
+    for n in ("bfs_graph_upload", "bfs_run", "bfs_run_roots", "bfs_run_device", "bfs_graph_free",
               "bfs_dataset_load", "bfs_gen_rmat_host", "bfs_validate_device"):
         assert n in names
 
@@ -63,3 +63,6 @@ def test_argument_errors_without_gpu(B):
     assert L.bfs_graph_upload(ip.ctypes.data_as(B.U32P), ip.ctypes.data_as(B.U32P), 3, 2, 0, 0,
                               C.byref(h)) == 1  # n_rows > n_cols
     assert L.bfs_run(None, 0, None, None, None, None) == 1
+    assert L.bfs_run_roots(None, None, 0, None, None, None, None) == 1
+    roots = np.zeros(2, np.uint32)
+    assert L.bfs_run_roots(None, roots.ctypes.data_as(B.U32P), 2, None, None, None, None) == 1

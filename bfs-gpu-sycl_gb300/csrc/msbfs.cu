@@ -350,6 +350,15 @@ __device__ __forceinline__ uint32_t nibble_to_bytes(uint32_t n) {
   return (n * 0x00204081u) & 0x01010101u;
 }
 
+// Byte i of x, sign-extended: one prmt whose selector copies byte i into the
+// low byte and replicates its sign bit (selector value 8 + i) into the others.
+__device__ __forceinline__ int32_t sext_byte(uint32_t x, int i) {
+  const uint32_t sel = (uint32_t)i | ((8u + (uint32_t)i) * 0x1110u);
+  uint32_t r;
+  asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "r"(sel));
+  return (int32_t)r;
+}
+
 template <int H>
 __device__ __forceinline__ void ms_store_rows(int32_t *__restrict__ row, size_t n, uint32_t v,
                                               bool in, uint32_t nl, uint32_t r, uint32_t b0,
@@ -366,7 +375,7 @@ __device__ __forceinline__ void ms_store_rows(int32_t *__restrict__ row, size_t 
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       if ((uint32_t)(H * 32 + j + i) >= nl) break;  // uniform
-      if (in) row[v] = (int32_t)(int8_t)(packed >> (8 * i));
+      if (in) row[v] = sext_byte(packed, i);
       row += n;
     }
   }
@@ -376,6 +385,7 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
                                                                 int final) {
   static_assert(kHistLevels <= 16, "levels must fit four bit planes");
   __shared__ unsigned long long s_edges[kLanes];
+  __shared__ unsigned long long s_common;
   const uint32_t lvl = st->lvl;
   const bool expand = final ? (lvl < kHistLevels) : (lvl + 1u == kHistLevels && st->F > 0);
   if (!final && !expand) return;  // uniform over the grid
@@ -388,23 +398,44 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   if (final) {
     if (threadIdx.x < kLanes) s_edges[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_common = 0;
     __syncthreads();
   }
+  const unsigned long long all_roots = nl >= 64u ? ~0ull : (1ull << nl) - 1ull;
   unsigned long long acc_lo = 0, acc_hi = 0;  // degree sums of roots lane, 32 + lane
+  unsigned long long common = 0;              // degree sums of vertices every root reached
   const uint64_t stride = (uint64_t)gridDim.x * kMsBlock;
   for (uint64_t t0 = (uint64_t)blockIdx.x * kMsBlock + warp * 32u; t0 < n; t0 += stride) {
     const uint32_t v = (uint32_t)t0 + lane;
     const bool in = v < n;
+    // this step's loads are issued together: the mask and degree for the
+    // edge counts, and history levels 0 .. 7 (8 .. 15 after them, if the
+    // search went that deep)
+    unsigned long long vm = 0;
+    uint32_t d = 0;
+    if (final && in) {
+      vm = vis[v];
+      if (v < n_rows) d = indptr[v + 1] - indptr[v];
+    }
     if (expand) {
       unsigned long long r = 0, p0 = 0, p1 = 0, p2 = 0, p3 = 0;
       if (in) {
-        for (uint32_t L = 0; L <= lmax; L++) {
-          const unsigned long long m = hist[(size_t)L * n + v];
-          r |= m;
-          p0 |= m & (0ull - (L & 1u));
-          p1 |= m & (0ull - ((L >> 1) & 1u));
-          p2 |= m & (0ull - ((L >> 2) & 1u));
-          p3 |= m & (0ull - ((L >> 3) & 1u));
+        // within levels L0 .. L0 + 3 (L0 a multiple of 4) bits 0 and 1 of
+        // the level are those of k, bits 2 and 3 those of L0
+        for (uint32_t L0 = 0; L0 <= lmax; L0 += 8) {
+          unsigned long long m[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++)
+            m[k] = (L0 + k <= lmax) ? hist[(size_t)(L0 + k) * n + v] : 0ull;
+#pragma unroll
+          for (int h = 0; h < 8; h += 4) {
+            const unsigned long long all4 = m[h] | m[h + 1] | m[h + 2] | m[h + 3];
+            r |= all4;
+            p0 |= m[h + 1] | m[h + 3];
+            p1 |= m[h + 2] | m[h + 3];
+            if ((L0 + h) & 4u) p2 |= all4;
+            if ((L0 + h) & 8u) p3 |= all4;
+          }
         }
       }
       ms_store_rows<0>(level, n, v, in, nl, (uint32_t)r, (uint32_t)p0, (uint32_t)p1,
@@ -418,10 +449,13 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
       // per-root degree sums as a bit-matrix product: lane j takes the
       // vertex masks of roots j and 32 + j (32 ballots), and the degrees go
       // in bit planes (one ballot per degree bit)
-      const unsigned long long vm = in ? vis[v] : 0ull;
-      const uint32_t deg = (in && v < n_rows && vm) ? indptr[v + 1] - indptr[v] : 0u;
+      const uint32_t deg = vm ? d : 0u;
       const uint32_t dmax = __reduce_max_sync(kFull, deg);
-      if (dmax) {
+      // the usual warp: every vertex with edges was reached by every root
+      // (the giant component), so its degrees count once for all roots
+      if (dmax && __all_sync(kFull, deg == 0u || vm == all_roots)) {
+        common += __reduce_add_sync(kFull, deg);
+      } else if (dmax) {
         const uint32_t lo = (uint32_t)vm, hi = (uint32_t)(vm >> 32);
         uint32_t mlo = 0, mhi = 0;
 #pragma unroll
@@ -445,9 +479,10 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
   if (final) {
     if (acc_lo) atomicAdd(&s_edges[lane], acc_lo);
     if (acc_hi) atomicAdd(&s_edges[32 + lane], acc_hi);
+    if (lane == 0 && common) atomicAdd(&s_common, common);
     __syncthreads();
-    if (threadIdx.x < nl && s_edges[threadIdx.x])
-      atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x]);
+    if (threadIdx.x < nl && s_edges[threadIdx.x] + s_common)
+      atomicAdd(&st->edges[threadIdx.x], s_edges[threadIdx.x] + s_common);
     if (blockIdx.x == 0 && threadIdx.x == 0) st->launches += 1;
   }
 }

@@ -330,7 +330,7 @@ static cudaError_t add_kernel(cudaGraph_t graph, cudaGraphNode_t *node,
 }
 
 // Builds the device-side level loop:
-//   memset(bitmaps) -> fill(levels/parents) -> init(root) -> while(F > 0) {
+//   fill(levels/parents, bitmaps) -> init(root) -> while(F > 0) {
 //     explore -> levelgen (last block sets the while condition) }
 // With a fixed arm the explore node is that arm's kernel.  With arm < 0
 // (learned schedule) it is explore_any, which runs the arm in st->arm: the

@@ -6,26 +6,28 @@
 // every vertex, writes levels and appends the new frontier with one atomic per
 // vertex.  The same two-step structure is kept here, redesigned for GB300:
 //
-//   explore   frontier queue entries carry {beg, end} of their edge range, so
-//             the per-level indptr gather moves out of the edge loop.  Edges
-//             are processed in warp rounds of 32 consecutive edges (coalesced
-//             reads of the edge array, streamed with an L2 evict-first policy
-//             and no L1 allocation).  The owner entry of each edge is resolved
-//             with a warp OR-reduction of entry boundaries plus popc instead of
-//             a per-edge binary search (:448-464, :336-346).
-//             Visiting tests one bit of a visited bitmap (n/8 bytes, pinned in
-//             L2 through an access-policy window) with a plain load and only
-//             then claims it with atomicOr, instead of byte masks.
+//   explore   a frontier queue entry carries its first edge and the exclusive
+//             prefix of degrees in queue order (plus its vertex id when
+//             parents are recorded), so the per-level indptr gather moves out
+//             of the edge loop.  Edges are processed in warp rounds of 32
+//             consecutive edges (coalesced reads of the edge array, streamed
+//             with an L2 evict-first policy and no L1 allocation).  The owner
+//             entry of each edge is resolved with a warp OR-reduction of entry
+//             boundaries plus popc instead of a per-edge binary search
+//             (:448-464, :336-346).  Visiting tests one bit of a visited
+//             bitmap (n/8 bytes, pinned in L2 through an access-policy window)
+//             with a plain load and only then claims it with atomicOr, instead
+//             of byte masks.
 //   levelgen  scans the bitmap words (n/32, not n bytes): new = vis & ~prev.
-//             Per warp: ballot over the 32 bits of each non-empty word,
-//             popc for positions, one reduction per word for degrees, one
-//             atomic per block for the queue tail.  The atomic adds
-//             (count << 32 | degree sum), so every entry also receives the
-//             exclusive prefix of degrees in queue order: the grid-wide scan
-//             that GLB needs comes out of the same atomic.
-//             Zero-degree vertices and vertices >= n_rows get their level but
-//             are not queued (they would expand nothing; run_bfs_cpu.hpp:31
-//             never expands tid >= numRows).
+//             Blocks claim spans of words from a counter; each warp lists its
+//             words' new vertices in shared memory, writes their levels and
+//             loads their degrees 32 at a time, and one atomic per block and
+//             span reserves the queue tail.  The atomic adds (count << 32 |
+//             degree sum), so every entry also receives the exclusive prefix
+//             of degrees in queue order: the grid-wide scan that GLB needs
+//             comes out of the same atomic.  Zero-degree vertices and vertices
+//             >= n_rows get their level but are not queued (they would expand
+//             nothing; run_bfs_cpu.hpp:31 never expands tid >= numRows).
 //   finish    the last level-generation block swaps the queues, accumulates
 //             edgesCount and, in the CUDA-graph loop, sets the while-node
 //             condition, so no host round trip happens between levels.

@@ -9,7 +9,9 @@
 // {explore, level generation} until the last level-generation block reports
 // an empty frontier.  A host-driven loop with the reference's per-level
 // read-back is kept as BFS_LOOP_HOST (it is also what the per-level recorder
-// of the learned scheduler uses).
+// of the learned scheduler uses).  bfs_run_roots runs the reference's
+// num_runs loop in one call: each run's level array goes to the host on a
+// second stream while the next run proceeds.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -18,6 +18,14 @@ __device__ __forceinline__ uint32_t ld_stream(const uint32_t *p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
+// Fire-and-forget OR into global memory (a reduction: no value comes back,
+// so nothing is written back to the registers of the issuing warp).
+__device__ __forceinline__ void red_or(uint32_t *p, uint32_t v) {
+  asm volatile("red.relaxed.gpu.global.or.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_or(unsigned long long *p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ uint64_t evict_first_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));

@@ -51,7 +51,7 @@ __device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent
     const uint32_t old = atomicOr(vis + w, bit);
     if (!(old & bit)) parent[n] = (int32_t)from;
   } else {
-    atomicOr(vis + w, bit);  // result unused: a reduction, no round trip
+    red_or(vis + w, bit);  // result unused: a reduction, no round trip
   }
 }
 

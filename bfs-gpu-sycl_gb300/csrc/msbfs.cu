@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
         // edge already gave v in this level: most edges of a dense level end
         // at one of the two tests, and the atomic runs only for new roots
         const unsigned long long bits = msk[u] & ~vis[nb[u]];
-        if (bits) atomicOr(vis + nb[u], bits);
+        if (bits) red_or(vis + nb[u], bits);
       }
     }
   }

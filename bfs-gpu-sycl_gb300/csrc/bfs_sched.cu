@@ -32,6 +32,7 @@
 #include "engine.h"
 #include "kernels.h"
 #include "bfs_sched.h"
+#include "dev_alloc.h"
 #include "bfs_sched_dev.cuh"
 
 namespace bfsgb {
@@ -266,9 +267,9 @@ bfs_status bfs_sched_record(bfs_graph *g, uint32_t root, int32_t ipt, int32_t re
   LevelTimer timer;
   bfs_options o;
   SK(cudaSetDevice(g->device));
-  SK(cudaMalloc(&ctx.backup, (size_t)g->words * 4));
-  SK(cudaMalloc(&ctx.d_feat, sizeof(float) * kSchedIn));
-  SK(cudaMalloc(&levels, sizeof(int32_t) * (size_t)g->n_cols));
+  SK(dev_malloc(&ctx.backup, (size_t)g->words * 4));
+  SK(dev_malloc(&ctx.d_feat, sizeof(float) * kSchedIn));
+  SK(dev_malloc(&levels, sizeof(int32_t) * (size_t)g->n_cols));
   SK(cudaEventCreate(&ctx.e0));
   SK(cudaEventCreate(&ctx.e1));
   timer.ctx = &ctx;
@@ -336,13 +337,13 @@ bfs_status bfs_sched_train(const bfs_level_sample *samples, uint32_t n,
   const double b1 = 0.9, b2 = 0.999;
   float loss = 0.f;
   SK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  SK(cudaMalloc(&d_w, sizeof(float) * kSchedParams));
-  SK(cudaMalloc(&d_g, sizeof(float) * kSchedParams));
-  SK(cudaMalloc(&d_m, sizeof(float) * kSchedParams));
-  SK(cudaMalloc(&d_v, sizeof(float) * kSchedParams));
-  SK(cudaMalloc(&d_X, sizeof(float) * X.size()));
-  SK(cudaMalloc(&d_C, sizeof(float) * Cst.size()));
-  SK(cudaMalloc(&d_loss, sizeof(float)));
+  SK(dev_malloc(&d_w, sizeof(float) * kSchedParams));
+  SK(dev_malloc(&d_g, sizeof(float) * kSchedParams));
+  SK(dev_malloc(&d_m, sizeof(float) * kSchedParams));
+  SK(dev_malloc(&d_v, sizeof(float) * kSchedParams));
+  SK(dev_malloc(&d_X, sizeof(float) * X.size()));
+  SK(dev_malloc(&d_C, sizeof(float) * Cst.size()));
+  SK(dev_malloc(&d_loss, sizeof(float)));
   SK(cudaMemcpyAsync(d_w, w0.data(), sizeof(float) * kSchedParams, cudaMemcpyHostToDevice, st));
   SK(cudaMemsetAsync(d_g, 0, sizeof(float) * kSchedParams, st));
   SK(cudaMemsetAsync(d_m, 0, sizeof(float) * kSchedParams, st));
@@ -382,10 +383,10 @@ bfs_status bfs_sched_predict(const float *weights, const float *features, uint32
   bfs_status rc = BFS_OK;
   float *d_w = nullptr, *d_X = nullptr, *d_conf = nullptr;
   int32_t *d_arms = nullptr;
-  SK(cudaMalloc(&d_w, sizeof(float) * kSchedParams));
-  SK(cudaMalloc(&d_X, sizeof(float) * (size_t)n * kSchedIn));
-  SK(cudaMalloc(&d_arms, sizeof(int32_t) * n));
-  SK(cudaMalloc(&d_conf, sizeof(float) * n));
+  SK(dev_malloc(&d_w, sizeof(float) * kSchedParams));
+  SK(dev_malloc(&d_X, sizeof(float) * (size_t)n * kSchedIn));
+  SK(dev_malloc(&d_arms, sizeof(int32_t) * n));
+  SK(dev_malloc(&d_conf, sizeof(float) * n));
   SK(cudaMemcpy(d_w, weights, sizeof(float) * kSchedParams, cudaMemcpyHostToDevice));
   SK(cudaMemcpy(d_X, features, sizeof(float) * (size_t)n * kSchedIn, cudaMemcpyHostToDevice));
   predict_kernel<<<std::min<uint32_t>(1024, (n + 7) / 8), 256>>>(d_w, d_X, n, d_arms, d_conf);
@@ -411,7 +412,7 @@ bfs_status bfs_sched_attach(bfs_graph *g, const float *weights, float min_confid
     if (!std::isfinite(weights[i])) return fail(BFS_ERR_INVALID_ARG, "non-finite weight");
   if (!g->sched) g->sched = new SchedModel();
   if (!g->sched->d_w) {
-    cudaError_t e = cudaMalloc(&g->sched->d_w, sizeof(float) * kSchedParams);
+    cudaError_t e = dev_malloc(&g->sched->d_w, sizeof(float) * kSchedParams);
     if (e != cudaSuccess) return fail(BFS_ERR_OOM, "scheduler weights");
   }
   if (cudaMemcpy(g->sched->d_w, weights, sizeof(float) * kSchedParams, cudaMemcpyHostToDevice) !=

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "bfs_internal.h"
+#include "dev_alloc.h"
 #include "engine.h"
 #include "kernels.h"
 #include "bfs_sched.h"
@@ -120,7 +121,7 @@ static bfs_status setup_workspace(bfs_graph *g) {
   const size_t q4 = align_up(nq * 4, 256), qp4 = align_up((nq + 1) * 4, 256);
   const size_t rec = align_up((size_t)BFS_MAX_RECORDED_LEVELS * 4, 256);
   g->ws_bytes = 2 * bm + 2 * (2 * q4 + qp4) + 4 * rec;
-  CK(cudaMalloc(&g->ws, g->ws_bytes));
+  CK(dev_malloc(&g->ws, g->ws_bytes));
   char *p = (char *)g->ws;
   BfsDevState &s = g->tmpl;
   std::memset(&s, 0, sizeof(s));
@@ -144,7 +145,7 @@ static bfs_status setup_workspace(bfs_graph *g) {
   s.fixed_arm = 0;
   s.level_cap = g->n_cols + 1u;
   g->bitmap_bytes = 2 * bm;
-  CK(cudaMalloc(&g->d_st, sizeof(BfsDevState)));
+  CK(dev_malloc(&g->d_st, sizeof(BfsDevState)));
   CK(cudaMallocHost(&g->h_st, sizeof(BfsDevState)));
 
   // persistent grid sizes (occupancy x SMs)
@@ -210,7 +211,7 @@ static bfs_status make_graph(const uint32_t *d_indptr, const uint32_t *d_inds,
   bfs_status rc = setup_workspace(g);
   if (rc == BFS_OK && validate) {
     unsigned long long *bad = nullptr, h_bad = 0;
-    cudaError_t e = cudaMalloc(&bad, sizeof(*bad));
+    cudaError_t e = dev_malloc(&bad, sizeof(*bad));
     if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(*bad), g->stream);
     if (e == cudaSuccess) e = launch_check_csc(g->indptr, g->inds, n_cols, nnz, bad, g->stream);
     if (e == cudaSuccess)
@@ -218,7 +219,8 @@ static bfs_status make_graph(const uint32_t *d_indptr, const uint32_t *d_inds,
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     cudaFree(bad);
     if (e != cudaSuccess)
-      rc = fail(BFS_ERR_CUDA, std::string("CSC check: ") + cudaGetErrorString(e));
+      rc = fail(e == cudaErrorMemoryAllocation ? BFS_ERR_OOM : BFS_ERR_CUDA,
+                std::string("CSC check: ") + cudaGetErrorString(e));
     else if (h_bad)
       rc = fail(BFS_ERR_GRAPH, "malformed CSC: " + std::to_string(h_bad) +
                                    " bad offsets or destinations");
@@ -652,8 +654,8 @@ bfs_status bfs_graph_upload(const uint32_t *indptr, const uint32_t *inds, uint32
   rc = require_device();
   if (rc != BFS_OK) return rc;
   uint32_t *d_indptr = nullptr, *d_inds = nullptr;
-  cudaError_t e = cudaMalloc(&d_indptr, sizeof(uint32_t) * ((size_t)n_cols + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&d_inds, sizeof(uint32_t) * (nnz ? nnz : 1));
+  cudaError_t e = dev_malloc(&d_indptr, sizeof(uint32_t) * ((size_t)n_cols + 1));
+  if (e == cudaSuccess) e = dev_malloc(&d_inds, sizeof(uint32_t) * (nnz ? nnz : 1));
   if (e == cudaSuccess)
     e = cudaMemcpy(d_indptr, indptr, sizeof(uint32_t) * ((size_t)n_cols + 1),
                    cudaMemcpyHostToDevice);
@@ -722,8 +724,8 @@ bfs_status bfs_run(bfs_graph *g, uint32_t root, const bfs_options *opts, int32_t
   if (!g || !levels_host) return fail(BFS_ERR_INVALID_ARG, "null graph or level buffer");
   CK(cudaSetDevice(g->device));
   const size_t bytes = sizeof(int32_t) * (size_t)g->n_cols;
-  if (!g->d_out_levels) CK(cudaMalloc(&g->d_out_levels, bytes));
-  if (parents_host && !g->d_out_parents) CK(cudaMalloc(&g->d_out_parents, bytes));
+  if (!g->d_out_levels) CK(dev_malloc(&g->d_out_levels, bytes));
+  if (parents_host && !g->d_out_parents) CK(dev_malloc(&g->d_out_parents, bytes));
   bfs_status rc = run_device_impl(g, root, opts, g->d_out_levels,
                                   parents_host ? g->d_out_parents : nullptr, stats, nullptr);
   if (rc != BFS_OK) return rc;
@@ -746,7 +748,7 @@ static bfs_status run_roots_impl(bfs_graph *g, const uint32_t *roots, uint32_t n
   const int kinds = parents_host ? 2 : 1;
   for (int slot = 0; slot < (n_roots > 1 ? 2 : 1); slot++)
     for (int k = 0; k < kinds; k++)
-      if (!g->d_ring[slot][k]) CK(cudaMalloc(&g->d_ring[slot][k], bytes));
+      if (!g->d_ring[slot][k]) CK(dev_malloc(&g->d_ring[slot][k], bytes));
   if (!g->copy_stream) CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
   if (!g->ev_ready) CK(cudaEventCreateWithFlags(&g->ev_ready, cudaEventDisableTiming));
   for (auto &e : g->ev_copied)
@@ -808,8 +810,8 @@ bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *level
   CK(cudaSetDevice(g->device));
   uint8_t *flags = nullptr;
   unsigned long long *d_bad = nullptr, h_bad = 0;
-  cudaError_t e = cudaMalloc(&flags, 2 * (size_t)g->n_cols);
-  if (e == cudaSuccess) e = cudaMalloc(&d_bad, sizeof(*d_bad));
+  cudaError_t e = dev_malloc(&flags, 2 * (size_t)g->n_cols);
+  if (e == cudaSuccess) e = dev_malloc(&d_bad, sizeof(*d_bad));
   if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 2 * (size_t)g->n_cols, g->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(*d_bad), g->stream);
   if (e == cudaSuccess)
@@ -830,7 +832,7 @@ bfs_status bfs_validate_host(bfs_graph *g, uint32_t root, const int32_t *levels_
   if (!g || !levels_host || !bad) return fail(BFS_ERR_INVALID_ARG, "null pointer");
   CK(cudaSetDevice(g->device));
   const size_t bytes = sizeof(int32_t) * (size_t)g->n_cols;
-  if (!g->d_out_levels) CK(cudaMalloc(&g->d_out_levels, bytes));
+  if (!g->d_out_levels) CK(dev_malloc(&g->d_out_levels, bytes));
   CK(cudaMemcpy(g->d_out_levels, levels_host, bytes, cudaMemcpyHostToDevice));
   return bfs_validate_device(g, root, g->d_out_levels, nullptr, bad);
 }

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bfs_internal.h"
+#include "dev_alloc.h"
 
 namespace bfsgb {
 bfs_status graph_from_owned_device(uint32_t *d_indptr, uint32_t *d_inds,
@@ -303,9 +304,9 @@ bfs_status bfs_gen_rmat_device(uint32_t scale, uint32_t edge_factor, double a,
     }                                                                \
   } while (0)
   GEN_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
-  GEN_CHECK(cudaMalloc(&k0, nk * sizeof(unsigned long long)), "keys");
-  GEN_CHECK(cudaMalloc(&k1, nk * sizeof(unsigned long long)), "keys");
-  GEN_CHECK(cudaMalloc(&d_nsel, sizeof(unsigned long long)), "count");
+  GEN_CHECK(dev_malloc(&k0, nk * sizeof(unsigned long long)), "keys");
+  GEN_CHECK(dev_malloc(&k1, nk * sizeof(unsigned long long)), "keys");
+  GEN_CHECK(dev_malloc(&d_nsel, sizeof(unsigned long long)), "count");
   {
     cub::DoubleBuffer<unsigned long long> db(k0, k1);
     GEN_CHECK(cub::DeviceRadixSort::SortKeys(nullptr, tmp_sort, db, (int64_t)nk, 0,
@@ -314,7 +315,7 @@ bfs_status bfs_gen_rmat_device(uint32_t scale, uint32_t edge_factor, double a,
     GEN_CHECK(cub::DeviceSelect::Unique(nullptr, tmp_uniq, k0, k1, d_nsel,
                                         (int64_t)nk, st),
               "unique sizing");
-    GEN_CHECK(cudaMalloc(&tmp, std::max(tmp_sort, tmp_uniq)), "cub temp");
+    GEN_CHECK(dev_malloc(&tmp, std::max(tmp_sort, tmp_uniq)), "cub temp");
     rmat_keys_kernel<<<2048, 256, 0, st>>>(p, symmetrize, k0);
     GEN_CHECK(cudaGetLastError(), "rmat keys");
     size_t ts = tmp_sort;
@@ -339,8 +340,8 @@ bfs_status bfs_gen_rmat_device(uint32_t scale, uint32_t edge_factor, double a,
       rc = fail(BFS_ERR_UNSUPPORTED, "graph has more than BFS_MAX_EDGES edges");
       goto done;
     }
-    GEN_CHECK(cudaMalloc(&indptr, sizeof(uint32_t) * ((size_t)n + 1)), "indptr");
-    GEN_CHECK(cudaMalloc(&inds, sizeof(uint32_t) * (nnz ? nnz : 1)), "inds");
+    GEN_CHECK(dev_malloc(&indptr, sizeof(uint32_t) * ((size_t)n + 1)), "indptr");
+    GEN_CHECK(dev_malloc(&inds, sizeof(uint32_t) * (nnz ? nnz : 1)), "inds");
     csc_from_keys_kernel<<<4096, 256, 0, st>>>(uniq, nnz, scale, n, indptr, inds);
     GEN_CHECK(cudaGetLastError(), "csc build");
     GEN_CHECK(cudaStreamSynchronize(st), "csc build");

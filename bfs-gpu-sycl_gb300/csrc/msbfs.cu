@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "bfs_internal.h"
+#include "dev_alloc.h"
 #include "device_util.cuh"
 #include "engine.h"
 #include "kernels.h"
@@ -540,8 +541,8 @@ static bfs_status ms_setup(bfs_graph *g) {
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t b64 = al(n * 8), q4 = al(nr * 4), qp4 = al((nr + 1) * 4), q8 = al(nr * 8);
   const size_t bytes = (2 + kHistLevels) * b64 + 2 * (q4 + qp4 + q8);
-  MK(cudaMalloc(&w->mem, bytes));
-  MK(cudaMalloc(&w->d_st, sizeof(MsState)));
+  MK(dev_malloc(&w->mem, bytes));
+  MK(dev_malloc(&w->d_st, sizeof(MsState)));
   MK(cudaMallocHost(&w->h_st, sizeof(MsState)));
   MK(cudaEventCreate(&w->e0));
   MK(cudaEventCreate(&w->e1));
@@ -731,7 +732,7 @@ extern "C" bfs_status bfs_run_batch_host(bfs_graph *g, const uint32_t *roots, ui
   }
   MsWorkspace *w = g->ms;
   const size_t n = g->n_cols;
-  if (!w->rows) MK(cudaMalloc(&w->rows, sizeof(int32_t) * n * kLanes));
+  if (!w->rows) MK(dev_malloc(&w->rows, sizeof(int32_t) * n * kLanes));
   bfs_batch_stats total;
   std::memset(&total, 0, sizeof(total));
   for (uint32_t b0 = 0; b0 < n_roots; b0 += kLanes) {

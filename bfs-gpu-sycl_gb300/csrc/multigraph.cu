@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "bfs_internal.h"
+#include "dev_alloc.h"
 #include "device_util.cuh"
 
 namespace bfsgb {
@@ -427,13 +428,13 @@ static bfs_status multi_prepare(bfs_multi *m, int cfg, int32_t *levels_dev) {
     if (m->gbits_words < n_clusters * words) {
       cudaFree(m->d_gbits);
       m->d_gbits = nullptr;
-      GK(cudaMalloc(&m->d_gbits, sizeof(uint32_t) * n_clusters * words));
+      GK(dev_malloc(&m->d_gbits, sizeof(uint32_t) * n_clusters * words));
       m->gbits_words = n_clusters * words;
     }
     if (m->gcnt_words < n_clusters * 4) {
       cudaFree(m->d_gcnt);
       m->d_gcnt = nullptr;
-      GK(cudaMalloc(&m->d_gcnt, sizeof(uint32_t) * n_clusters * 4));
+      GK(dev_malloc(&m->d_gcnt, sizeof(uint32_t) * n_clusters * 4));
       m->gcnt_words = n_clusters * 4;
     }
   } else {
@@ -565,16 +566,16 @@ bfs_status bfs_multi_create(uint32_t n_graphs, const uint32_t *const *indptrs,
   CK2(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
   CK2(cudaEventCreate(&m->e0));
   CK2(cudaEventCreate(&m->e1));
-  CK2(cudaMalloc(&m->d_indptr, sizeof(uint32_t) * vb));
-  CK2(cudaMalloc(&m->d_inds, sizeof(uint32_t) * std::max<uint64_t>(eb, 1)));
-  CK2(cudaMalloc(&m->d_order, sizeof(uint32_t) * n_graphs));
-  CK2(cudaMalloc(&m->d_work, 2 * sizeof(uint32_t)));
-  CK2(cudaMalloc(&m->d_descs, sizeof(MultiDesc) * n_graphs));
-  CK2(cudaMalloc(&m->d_edges, sizeof(unsigned long long) * n_graphs));
+  CK2(dev_malloc(&m->d_indptr, sizeof(uint32_t) * vb));
+  CK2(dev_malloc(&m->d_inds, sizeof(uint32_t) * std::max<uint64_t>(eb, 1)));
+  CK2(dev_malloc(&m->d_order, sizeof(uint32_t) * n_graphs));
+  CK2(dev_malloc(&m->d_work, 2 * sizeof(uint32_t)));
+  CK2(dev_malloc(&m->d_descs, sizeof(MultiDesc) * n_graphs));
+  CK2(dev_malloc(&m->d_edges, sizeof(unsigned long long) * n_graphs));
   // queues: two of max_rows entries per resident block (bounded by the
   // largest occupancy of any configuration)
   m->queue_blocks = (size_t)m->num_sms * 16;
-  CK2(cudaMalloc(&m->d_queues, sizeof(uint32_t) * 2 * (size_t)m->max_rows * m->queue_blocks));
+  CK2(dev_malloc(&m->d_queues, sizeof(uint32_t) * 2 * (size_t)m->max_rows * m->queue_blocks));
   CK2(cudaMemcpy(m->d_indptr, hip.data(), sizeof(uint32_t) * vb, cudaMemcpyHostToDevice));
   CK2(cudaMemcpy(m->d_inds, hix.data(), sizeof(uint32_t) * std::max<uint64_t>(eb, 1),
                  cudaMemcpyHostToDevice));

@@ -22,7 +22,8 @@
  *     vertices, otherwise the hop distance (src/host.cpp:113-115).
  *   - No function throws; every one returns a bfs_status.  bfs_last_error()
  *     gives a message for the most recent failure on the calling thread.
- *   - Each graph handle owns one CUDA stream; calls on one handle must not
+ *   - Each graph handle owns its CUDA streams (one for the BFS kernels, one
+ *     for bfs_run_roots' copies to the host); calls on one handle must not
  *     overlap from several host threads.
  */
 #ifndef BFS_GB300_H

@@ -196,9 +196,9 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
 #pragma unroll
       for (int u = 0; u < U; u++) {
         if (nb[u] == kFull) continue;
-        // roots that reached v before this level, then roots that another
-        // edge already gave v in this level: most edges of a dense level end
-        // at one of the two tests, and the atomic runs only for new roots
+        // roots not yet in v's live mask (it holds the roots of earlier levels
+        // and those other edges gave v in this level): only new roots cost a
+        // reduction
         const unsigned long long bits = msk[u] & ~vis[nb[u]];
         if (bits) red_or(vis + nb[u], bits);
       }

@@ -121,8 +121,10 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
 
 // Explore: the single-root GLB walk (one difference per entry, a 32-entry
 // window re-based only when a round could leave it) with a root mask per
-// entry: vis[v] |= mask(u) & ~vis[v].  The plain load may see a stale mask,
-// which costs only a redundant atomic.
+// entry: vis[v] |= mask(u) & ~vis[v].  A lane keeps its edge's entry index
+// and reads the entry's mask only when v is not yet reached by every root
+// (no mask travels through shuffles).  The plain load may see a stale mask,
+// which costs only a redundant reduction.
 __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     ms_explore_kernel(MsState *__restrict__ st) {
   constexpr int NW = kMsBlock / 32;
@@ -137,6 +139,7 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
   const unsigned long long *__restrict__ qm = st->qm[cq];
   const uint32_t *__restrict__ inds = st->inds;
   unsigned long long *vis = st->vis;
+  const unsigned long long all_roots = st->n_lanes >= 64u ? ~0ull : (1ull << st->n_lanes) - 1ull;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint64_t pol = evict_first_policy();
   const uint32_t total_warps = gridDim.x * NW;
@@ -151,15 +154,12 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
     uint32_t cur = warp_owner_search(qp, F, w0, lane);
     uint32_t cur_d = qb[cur] - qp[cur];
-    unsigned long long cur_mask = qm[cur];
     uint32_t c0 = cur;
     uint32_t bnd = (c0 + 1u + lane <= F) ? qp[c0 + 1u + lane] : kFull;
     uint32_t dl = (c0 + 1u + lane < F) ? qb[c0 + 1u + lane] - bnd : 0u;
-    unsigned long long mk = (c0 + 1u + lane < F) ? qm[c0 + 1u + lane] : 0ull;
     uint32_t wlast = __shfl_sync(kFull, bnd, 31);
     for (uint32_t base = w0; base < w1; base += kRound) {
-      uint32_t ad[U], nb[U];
-      unsigned long long msk[U];
+      uint32_t ad[U], nb[U], ent[U];
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
@@ -169,7 +169,6 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
           const uint32_t j = c0 + 1u + lane;
           bnd = (j <= F) ? qp[j] : kFull;
           dl = (j < F) ? qb[j] - bnd : 0u;
-          mk = (j < F) ? qm[j] : 0ull;
           wlast = __shfl_sync(kFull, bnd, 31);
         }
         const uint32_t p = bnd - rb;
@@ -177,18 +176,13 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
         const uint32_t k = __popc(starts & ((2u << lane) - 1u));
         const uint32_t srcl = k ? cur + k - c0 - 1u : 0u;
         const uint32_t s_d = __shfl_sync(kFull, dl, srcl);
-        const unsigned long long s_mask = __shfl_sync(kFull, mk, srcl);
         ad[u] = kFull;
-        msk[u] = 0;
-        if (e < w1) {
-          ad[u] = e + (k ? s_d : cur_d);
-          msk[u] = k ? s_mask : cur_mask;
-        }
+        ent[u] = cur + k;  // the edge's entry: its root mask is read only if needed
+        if (e < w1) ad[u] = e + (k ? s_d : cur_d);
         const uint32_t k31 = __popc(starts);
         if (k31) {
           cur += k31;
           cur_d = __shfl_sync(kFull, dl, cur - c0 - 1u);
-          cur_mask = __shfl_sync(kFull, mk, cur - c0 - 1u);
         }
       }
 #pragma unroll
@@ -198,8 +192,10 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
         if (nb[u] == kFull) continue;
         // roots not yet in v's live mask (it holds the roots of earlier levels
         // and those other edges gave v in this level): only new roots cost a
-        // reduction
-        const unsigned long long bits = msk[u] & ~vis[nb[u]];
+        // reduction.  A target every root has reached needs no root mask.
+        const unsigned long long vm = vis[nb[u]];
+        if (vm == all_roots) continue;
+        const unsigned long long bits = qm[ent[u]] & ~vm;
         if (bits) red_or(vis + nb[u], bits);
       }
     }

@@ -116,8 +116,6 @@ struct BfsDevState {
   float sched_min_conf;      // below this top probability: the fallback arm
   float sched_diam;          // graph-level feature constants
   float sched_avg_deg_x;
-  unsigned long long sched_cond0; // switch conditions to set with the arm (0: none)
-  unsigned long long sched_cond;
   // per-level record (first BFS_MAX_RECORDED_LEVELS levels)
   uint32_t *rec_frontier;
   uint32_t *rec_edges;

@@ -47,9 +47,9 @@ SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz) {
 }
 
 __global__ void sched_kernel(BfsDevState *st, const float *__restrict__ w, float min_conf,
-                             SchedGraphConst gc, unsigned long long cond, int use_cond) {
+                             SchedGraphConst gc) {
   if (threadIdx.x >= 32) return;
-  sched_pick_warp(st, w, min_conf, gc, cond, use_cond != 0);
+  sched_pick_warp(st, w, min_conf, gc);
   if (threadIdx.x == 0) st->launches += 1;
 }
 

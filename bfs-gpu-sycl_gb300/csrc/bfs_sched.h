@@ -34,11 +34,10 @@ struct SchedModel {
 
 SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz);
 
-// Kernel (one warp): reads the level's features from the device state, picks
-// an arm and stores it in st->arm and st->rec_arm[lvl]; with use_cond it also
-// sets the switch condition of the CUDA-graph level loop.
-// Arguments: (BfsDevState*, const float* w, float min_conf, SchedGraphConst,
-//             unsigned long long cond, int use_cond)
+// Kernel (one warp) of the host-driven level loop: reads the level's
+// features from the device state, picks an arm and stores it in st->arm and
+// st->rec_arm[lvl].
+// Arguments: (BfsDevState*, const float* w, float min_conf, SchedGraphConst)
 const void *sched_kernel_fn();
 
 }  // namespace bfsgb

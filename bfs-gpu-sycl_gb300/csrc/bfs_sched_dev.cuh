@@ -73,10 +73,9 @@ __device__ __forceinline__ float softmax9(float z, uint32_t lane, int *best, flo
 
 // One warp: the arm for the state's current level (kFallbackArm without a
 // model, on an empty frontier or below min_conf).  Lane 0 stores it in
-// st->arm and the level record, and with set_cond sets the switch condition.
+// st->arm and the level record.
 __device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__restrict__ w,
-                                               float min_conf, SchedGraphConst gc,
-                                               unsigned long long cond, bool set_cond) {
+                                               float min_conf, SchedGraphConst gc) {
   const uint32_t lane = threadIdx.x & 31u;
   int arm = kFallbackArm;
   if (w != nullptr && st->F > 0) {
@@ -91,7 +90,6 @@ __device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__r
   if (lane == 0) {
     st->arm = arm;
     if (st->lvl < st->rec_cap) st->rec_arm[st->lvl] = arm;
-    if (set_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, (unsigned)arm);
   }
   return arm;
 }

@@ -418,9 +418,7 @@ static bfs_status launch_sched(bfs_graph *g) {
   const float *w = g->sched ? g->sched->d_w : nullptr;
   float min_conf = g->sched ? g->sched->min_conf : 0.f;
   SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
-  unsigned long long no_cond = 0;
-  int zero = 0;
-  void *args[] = {&st, &w, &min_conf, &gc, &no_cond, &zero};
+  void *args[] = {&st, &w, &min_conf, &gc};
   CK(cudaLaunchKernel(sched_kernel_fn(), dim3(1), dim3(32), args, 0, g->stream));
   return BFS_OK;
 }

@@ -122,15 +122,13 @@ struct BlockIndex {
 
 // One warp: the learned scheduler's arm for the state's current level, from
 // the weights w (staged in shared memory by the caller) and the graph
-// constants held in the state, stored in st->arm for explore_any (and, if
-// sw != 0, set as switch condition sw).  Kept out of line so that the
-// callers' register allocation is not affected.
-__device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w,
-                                              unsigned long long sw, int use_cond) {
+// constants held in the state, stored in st->arm for explore_any.  Kept out
+// of line so that the callers' register allocation is not affected.
+__device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w) {
   SchedGraphConst gc;
   gc.diam = st->sched_diam;
   gc.avg_deg_x = st->sched_avg_deg_x;
-  sched_pick_warp(st, w, st->sched_min_conf, gc, sw, use_cond != 0 && sw != 0);
+  sched_pick_warp(st, w, st->sched_min_conf, gc);
 }
 
 // Copies the model to shared memory with all threads of the block: one
@@ -200,7 +198,7 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
   if (w != nullptr) stage_weights(s_w, w);
   if (threadIdx.x == 0) init_state(st, cond, use_cond);
   __syncwarp();
-  if (w != nullptr) fused_sched_pick(st, s_w, st->sched_cond0, use_cond);
+  if (w != nullptr) fused_sched_pick(st, s_w);
 }
 
 // ---- explore: LLB / SLB -----------------------------------------------------
@@ -722,7 +720,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       finish_level(st, cond, use_cond);
     }
     __syncthreads();
-    if (w != nullptr && warp == 0) fused_sched_pick(st, s_w, st->sched_cond, use_cond);
+    if (w != nullptr && warp == 0) fused_sched_pick(st, s_w);
   }
 }
 

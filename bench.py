@@ -438,8 +438,7 @@ def run_gb300(a):
         "ms_per_step": round(total_ms / len(dev_ms), 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic (seeded R-MAT generated on the device)",
-        "config": {"workload": f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, single-root "
-                   f"BFS, explore plan {plan}, {a.loop} level loop",
+        "config": {"workload": workload(a), "explore_plan": plan, "level_loop": a.loop,
                    "scheduler_weights": os.path.basename(WEIGHTS) if weights is not None
                    else None,
                    "vertices": n, "edges": dg.nnz, "roots_timed": a.steps,
@@ -480,19 +479,26 @@ def run_gb300(a):
     dg.free()
 
 
+def workload(a):
+    """The workload name both arms print in config.workload."""
+    return f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, single-root BFS"
+
+
 def run_reference(a):
     """The reference's CPU BFS (oracle port of run_bfs_cpu) on every host
-    thread, same workload; rank 0 only."""
+    thread, same workload; rank 0 only.  The graph and roots come from the
+    oracle's own restatement of the generator and root sampler (pinned to the
+    engine's bytes by tests/test_oracle_gen.py), so this arm never loads the
+    engine library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import bfs_gb300 as B
     import bfs_oracle as O
     nthreads = os.cpu_count() or 1
     t = time.perf_counter()
-    g = B.gen_rmat(a.scale, a.edge_factor, seed=a.seed)
+    g = O.oracle_gen_rmat(a.scale, a.edge_factor, seed=a.seed, threads=nthreads)
     gen_s = time.perf_counter() - t
-    roots = B.sample_roots(g, nthreads * (a.warmup + a.steps), a.seed)
+    roots = O.oracle_sample_roots(g.indptr, nthreads * (a.warmup + a.steps), a.seed)
     times, edges = [], []
     for s in range(a.warmup + a.steps):
         rs = roots[s * nthreads:(s + 1) * nthreads]
@@ -509,9 +515,8 @@ def run_reference(a):
            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
            "ms_per_step": round(1e3 * sum(times) / len(times), 2), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-           "data": "synthetic (seeded R-MAT, host generator)",
-           "config": {"workload": f"RMAT-{a.scale}/EF{a.edge_factor} seed {a.seed}, "
-                      f"single-root BFS", "vertices": g.n_cols, "edges": g.nnz,
+           "data": "synthetic (seeded R-MAT, the oracle's host generator)",
+           "config": {"workload": workload(a), "vertices": g.n_cols, "edges": g.nnz,
                       "graph_gen_s": round(gen_s, 2)},
            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthreads,
                             "kind": "port", "sample": sample},

@@ -30,7 +30,7 @@ std::string part_prefix(const char *dir, const char *name, uint32_t parts) {
   if (dir && dir[0]) {
     base = dir;
   } else {
-    const char *pwd = getenv("PWD");  // graph_load.hpp:184
+    const char *pwd = getenv("PWD");  // graph_load.hpp:98-101
     base = std::string(pwd ? pwd : ".") + "/dataset";
   }
   return base + "/" + name + "-csc-" + std::to_string(parts) + "/" + name + "-csc-";

@@ -16,6 +16,18 @@
 // host code is a host-side stand-in, not a device address, so it is never
 // passed to a kernel).  Make that first call before any stream capture.
 //
+// The first call is also when the array may come into existence.  Under
+// CUDA's default lazy module loading (CUDA_MODULE_LOADING=LAZY) the library's
+// device code and this array are loaded, and their device memory taken, when
+// a device first uses them -- that is, inside the first call.  So make one
+// warm-up call per device at start-up, outside any allocator callback and
+// before a memory budget is fixed; every later call allocates nothing.
+// Setting CUDA_MODULE_LOADING=EAGER instead loads the array when the context
+// is created.  The address looked up at set-up is kept for the life of the
+// process: after cudaDeviceReset, or with another context made current on
+// the same device, it is stale, and such a process must not call this entry
+// point again.
+//
 // Sharing: every call on a device uses the same array, and the array keeps the
 // previous call's contents; each call clears the parts that must start at zero
 // (both bitmaps and the loop counters).  Two calls that overlap on the GPU --

@@ -252,7 +252,14 @@ int32_t bfs_multi_num_configs(int32_t *blocks, int32_t *ipts, int32_t *clusters,
  * inside the library (about 24 MiB per GPU that loads it, held until exit),
  * so graphs are limited to BFS_NOALLOC_MAX_VERTICES vertices and larger ones
  * are rejected with BFS_ERR_INVALID_ARG.  The first call on a device looks
- * up that array's address (make it before any stream capture).  All calls on
+ * up that array's address (make it before any stream capture), and under
+ * CUDA's default lazy module loading it is also the call that loads the
+ * library's device code and the array, taking their device memory: make one
+ * warm-up call per device at start-up, outside any allocator callback and
+ * before a memory budget is fixed (or set CUDA_MODULE_LOADING=EAGER).  Later
+ * calls allocate nothing.  The address is kept for the life of the process,
+ * so a process that resets the device (cudaDeviceReset) or makes another
+ * context current on it must not call this entry point again.  All calls on
  * a device share the array: calls that overlap on the GPU race, so serialise
  * them.  stream may be NULL (default stream); the call returns when the BFS
  * has finished. */

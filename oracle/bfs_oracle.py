@@ -4,6 +4,10 @@
                   (src/run_bfs_cpu.hpp:5-85), see bfs_oracle.c
   ref_bfs      -- _ref/libref_bfs.so, the reference's own run_bfs_cpu compiled
                   in place by the Makefile (only where the reference exists)
+  oracle_gen_rmat, oracle_sample_roots
+               -- graph_gen_oracle.c, an independent restatement of the
+                  engine's seeded R-MAT generator and root sampler, so that
+                  the CPU baseline builds its inputs without the engine
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
 module; the engine never does.
@@ -49,6 +53,12 @@ def _load():
                                        C.c_uint32, I32P, U64P]
         L.oracle_bfs_multi.argtypes = [C.c_uint32, C.c_uint32, C.c_int, C.POINTER(U32P),
                                        C.POINTER(U32P), U64P, C.c_uint32, I32P, U64P]
+        L.oracle_gen_rmat.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                                      C.c_double, C.c_uint64, C.c_int, C.c_int,
+                                      C.POINTER(U32P), C.POINTER(U32P), U64P]
+        L.oracle_sample_roots.argtypes = [U32P, C.c_uint32, C.c_uint32, C.c_uint64, U32P]
+        L.oracle_free.argtypes = [C.c_void_p]
+        L.oracle_free.restype = None
         _lib = L
     return _lib
 
@@ -161,3 +171,46 @@ def ref_bfs(indptrs, indss, root, n_rows, n_cols):
     if rc != 0:
         raise ValueError(f"ref_bfs failed with status {rc}")
     return lv, ec.value
+
+
+class Csc:
+    """A CSC graph held in arrays that the oracle library allocated; each
+    buffer is released when the last numpy view of it is garbage collected."""
+
+    def __init__(self, indptr_p, inds_p, n, nnz):
+        self.n_rows = self.n_cols = n
+        self.nnz = nnz
+        self.indptr = _owned(indptr_p, n + 1)
+        self.inds = _owned(inds_p, max(nnz, 1))[:nnz]
+
+
+def _owned(ptr, count):
+    import weakref
+    base = np.ctypeslib.as_array(ptr, shape=(count,))
+    weakref.finalize(base, _load().oracle_free, C.cast(ptr, C.c_void_p).value)
+    return base
+
+
+def oracle_gen_rmat(scale, edge_factor, a=0.57, b=0.19, c=0.19, seed=1, symmetrize=True,
+                    threads=0):
+    """Seeded R-MAT CSC (deduplicated, self-loops dropped), built on the host
+    by graph_gen_oracle.c; the same bytes as the engine's generator."""
+    ip, ix, nnz = U32P(), U32P(), C.c_uint64(0)
+    rc = _load().oracle_gen_rmat(int(scale), int(edge_factor), float(a), float(b), float(c),
+                                 int(seed), int(bool(symmetrize)), int(threads), C.byref(ip),
+                                 C.byref(ix), C.byref(nnz))
+    if rc != 0:
+        raise ValueError(f"oracle_gen_rmat failed with status {rc}")
+    return Csc(ip, ix, 1 << int(scale), int(nnz.value))
+
+
+def oracle_sample_roots(indptr, count, seed, n_rows=None):
+    """count distinct seeded roots with out-degree > 0."""
+    ip = _arr(indptr, np.uint32)
+    n_rows = int(n_rows if n_rows is not None else len(ip) - 1)
+    out = np.empty(max(int(count), 1), np.uint32)
+    rc = _load().oracle_sample_roots(ip.ctypes.data_as(U32P), n_rows, int(count), int(seed),
+                                     out.ctypes.data_as(U32P))
+    if rc != 0:
+        raise ValueError(f"oracle_sample_roots failed with status {rc}")
+    return out[:int(count)]

@@ -19,8 +19,7 @@ def _ensure_built():
     import build as pkg_build  # bfs-gpu-sycl_gb300/build.py
     pkg_build.build(verbose=False)
     import bfs_oracle
-    if not os.path.exists(bfs_oracle.LIB):
-        bfs_oracle.build()
+    bfs_oracle.build()  # make rebuilds only what changed
 
 
 _ensure_built()

@@ -1,4 +1,6 @@
-"""Small, self-contained workloads for profiling single kernels with ncu.
+"""Profiling fixture (not collected by pytest, not part of the engine): small,
+self-contained workloads for profiling single kernels with ncu.  The commands
+recorded in profiles/*.md run it.
 
 Each case builds its input on the device from a fixed seed, runs the path once
 and prints what it ran, so that an ncu capture (`-k <kernel> -s <skip> -c <n>`)
@@ -18,14 +20,15 @@ sees a known sequence of launches:
                   (default 512 4 1).
 
 Examples:
-  python bfs-gpu-sycl_gb300/profile_case.py bfs 24 glb256
+  python tests/profile_case.py bfs 24 glb256
   ncu --set full --clock-control none -k regex:explore_global -s 2 -c 2 \\
-      -o prof python bfs-gpu-sycl_gb300/profile_case.py bfs 24 glb256
+      -o prof python tests/profile_case.py bfs 24 glb256
 """
 import os
 import sys
 
-sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                "bfs-gpu-sycl_gb300"))
 import torch  # noqa: E402
 
 import bfs_gb300 as B  # noqa: E402

@@ -90,3 +90,31 @@ def test_noalloc_rejects_oversized_and_bad_input(B):
     assert "at most 1048576 vertices" in msg
     assert f(None, None, 4, 4, 0, 0, out, None, None) == 1
     assert f(C.c_void_p(1), C.c_void_p(1), 4, 4, 0, 9, out, None, None) == 2  # root
+
+
+def test_noalloc_takes_no_device_memory_after_warmup(B, O, monkeypatch):
+    """The property the entry point exists for: once a warm-up call has
+    loaded the library's device code and array on this device, further calls
+    leave the device's free memory unchanged, and they still succeed when
+    every allocation through the engine's allocation hook is made to fail."""
+    torch = torch_cuda()
+    f = noalloc_fn(B)
+    g = B.gen_rmat(15, 16, seed=8)
+    ip = torch.from_numpy(g.indptr.view(np.int32)).cuda()
+    ix = torch.from_numpy(g.inds.view(np.int32)).cuda()
+    out = torch.empty(g.n_cols, dtype=torch.int32, device="cuda")
+    roots = B.sample_roots(g, 3, 8)
+    edges = C.c_uint64(0)
+    assert f(ip.data_ptr(), ix.data_ptr(), g.n_rows, g.n_cols, g.nnz, int(roots[0]),
+             out.data_ptr(), C.byref(edges), None) == 0  # warm-up
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    monkeypatch.setenv("BFS_GB300_FAIL_ALLOC_BYTES", "1")
+    for r in roots[1:]:
+        rc = f(ip.data_ptr(), ix.data_ptr(), g.n_rows, g.n_cols, g.nnz, int(r), out.data_ptr(),
+               C.byref(edges), None)
+        assert rc == 0, B.lib().bfs_last_error()
+        lv, ec = O.oracle_bfs(g.indptr, g.inds, int(r))
+        assert np.array_equal(out.cpu().numpy(), lv) and edges.value == ec
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before

@@ -111,6 +111,8 @@ def lib():
     _sig(L, "bfs_graph_free", [VP])
     _sig(L, "bfs_graph_info", [VP, U32P, U32P, C.POINTER(C.c_uint64)])
     _sig(L, "bfs_graph_device_csc", [VP, C.POINTER(VP), C.POINTER(VP)])
+    _sig(L, "bfs_hub_configure", [VP, C.c_int64, C.c_uint32])
+    _sig(L, "bfs_hub_info", [VP, U32P, I32P, U32P])
     _sig(L, "bfs_run", [VP, C.c_uint32, C.POINTER(Options), I32P, I32P, C.POINTER(Stats)])
     _sig(L, "bfs_run_device", [VP, C.c_uint32, C.POINTER(Options), VP, VP, C.POINTER(Stats)])
     _sig(L, "bfs_run_roots", [VP, U32P, C.c_uint32, C.POINTER(Options), C.POINTER(VP),
@@ -453,6 +455,18 @@ class Graph:
         ch = CscHost()
         check(lib().bfs_graph_download(self.h, C.byref(ch)))
         return Csc._from_c(ch)
+
+    def hub_configure(self, vertices=-1, min_edges=0):
+        """Hub layout of the single-root path: vertices -1 automatic, 0 off,
+        K > 0; min_edges: level size from which explore loads the prefix
+        (0 automatic)."""
+        check(lib().bfs_hub_configure(self.h, int(vertices), int(min_edges)))
+
+    def hub_info(self):
+        """(K, relabelled, largest K the device allows) of the current layout."""
+        k, rl, mx = C.c_uint32(), C.c_int32(), C.c_uint32()
+        check(lib().bfs_hub_info(self.h, C.byref(k), C.byref(rl), C.byref(mx)))
+        return k.value, bool(rl.value), mx.value
 
     def device_csc(self):
         ip, ix = VP(), VP()

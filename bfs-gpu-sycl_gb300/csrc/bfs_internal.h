@@ -6,9 +6,12 @@
 //   vis     u32[words]        visited bitmap, bit v = vertex v reached
 //   prev    u32[words]        visited bitmap as of the previous level
 //   qb[2]   u32[n_rows]       frontier queue: first edge (indptr[v]) of each entry
-//   qp[2]   u32[n_rows + 1]   exclusive prefix of entry degrees (queue order);
-//                             qp[F] holds the frontier's edge total
-//   qv[2]   u32[n_rows]       vertex id of each entry
+//   qd[2]   u32[n_rows]       degree of each entry
+//   qc[2]   u32[n_rows + 1]   exclusive prefix of entry chunk counts (queue
+//                             order): the 16-byte chunks of inds that hold an
+//                             entry's edges; qc[F] holds the chunk total
+//   qv[2]   u32[n_rows]       original vertex id of each entry (written only
+//                             when parents are recorded)
 //   state   BfsDevState       counters of the level loop (one struct)
 // words = ceil(n_cols / 32) rounded up to a multiple of 32 (one warp reads
 // 32 consecutive words in the level-generation kernel).
@@ -71,6 +74,13 @@ BFS_HD void rmat_edge(const RmatParams &p, uint64_t i, uint32_t *u_out,
   *v_out = v;
 }
 
+// 16-byte chunks of the edge array (4 uint32 entries each) that hold the
+// edges [b, b + deg) of one vertex, for an array starting off uint32 past a
+// 16-byte boundary: chunks (b + off)/4 .. (b + off + deg - 1)/4.
+BFS_HD uint32_t edge_chunks(uint32_t b, uint32_t deg, uint32_t off) {
+  return deg ? ((b + off + deg + 3u) >> 2) - ((b + off) >> 2) : 0u;
+}
+
 // Maps a 64-bit hash to [0, n).
 BFS_HD uint32_t hash_to_range(uint64_t h, uint32_t n) {
   return (uint32_t)(((h >> 32) * (uint64_t)n) >> 32);
@@ -81,6 +91,10 @@ struct BfsDevState {
   // graph
   const uint32_t *indptr;
   const uint32_t *inds;
+  uint32_t nnz;          // entries of inds (< 2^32)
+  uint32_t inds_off;     // inds' offset in uint32 from the 16-byte boundary
+                         // below it (0..3): edge p lies in 16-byte chunk
+                         // (p + inds_off) / 4 counted from that boundary
   uint32_t n_rows, n_cols;
   uint32_t words;        // bitmap words (padded)
   uint32_t root;
@@ -88,16 +102,26 @@ struct BfsDevState {
   uint32_t *vis;
   uint32_t *prev;
   uint32_t *qb[2];
-  uint32_t *qp[2];
+  uint32_t *qd[2];
+  uint32_t *qc[2];
   uint32_t *qv[2];
   int32_t *level;
   int32_t *parent;       // may be null
+  // hub layout (hub_layout.cu): with a relabelled graph, indptr/inds above are
+  // the relabelled CSC and the kernels work on internal ids; levels and
+  // parents are written in original ids.  Null: identity.
+  const uint32_t *perm;  // internal id -> original id
+  const uint32_t *pinv;  // original id -> internal id
+  uint32_t hub_words;    // bitmap words of the hub prefix kept in shared memory
+  uint32_t hub_min_edges;  // frontier edges from which explore loads them
   // level-loop counters (written by kernels)
-  unsigned long long next_packed;  // (count << 32) | degree sum, next frontier
+  unsigned long long next_packed;  // (count << 32) | chunk sum, next frontier
   unsigned long long edges_count;  // sum of degrees of expanded vertices
+  uint32_t next_edges;   // degree sum of the next frontier
   uint32_t cur;          // queue buffer holding the current frontier
   uint32_t F;            // current frontier entries
   uint32_t EF;           // current frontier edges
+  uint32_t EC;           // current frontier 16-byte chunks of inds
   uint32_t lvl;          // level of the current frontier
   uint32_t reached;      // vertices with a level
   uint32_t reached_prev; // `reached` before the current level generation

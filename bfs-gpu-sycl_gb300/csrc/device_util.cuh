@@ -18,6 +18,21 @@ __device__ __forceinline__ uint32_t ld_stream(const uint32_t *p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
+// 16-byte edge-array load (four consecutive entries), same cache policy.
+__device__ __forceinline__ uint4 ld_stream4(const uint4 *p, uint64_t pol) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p), "l"(pol));
+  return r;
+}
+// 1 << p for p < 32 and 0 for p >= 32 (PTX shl clamps the shift amount;
+// C++ would leave p >= 32 undefined).
+__device__ __forceinline__ uint32_t bit_or_zero(uint32_t p) {
+  uint32_t r;
+  asm("shl.b32 %0, 1, %1;" : "=r"(r) : "r"(p));
+  return r;
+}
 // Fire-and-forget OR into global memory (a reduction: no value comes back,
 // so nothing is written back to the registers of the issuing warp).
 __device__ __forceinline__ void red_or(uint32_t *p, uint32_t v) {

@@ -27,6 +27,7 @@
 #include "engine.h"
 #include "kernels.h"
 #include "bfs_sched.h"
+#include "hub_layout.h"
 
 namespace bfsgb {
 
@@ -120,13 +121,15 @@ static bfs_status setup_workspace(bfs_graph *g) {
   const size_t nq = std::max<size_t>(g->n_rows, 1);
   const size_t q4 = align_up(nq * 4, 256), qp4 = align_up((nq + 1) * 4, 256);
   const size_t rec = align_up((size_t)BFS_MAX_RECORDED_LEVELS * 4, 256);
-  g->ws_bytes = 2 * bm + 2 * (2 * q4 + qp4) + 4 * rec;
+  g->ws_bytes = 2 * bm + 2 * (3 * q4 + qp4) + 4 * rec;
   CK(dev_malloc(&g->ws, g->ws_bytes));
   char *p = (char *)g->ws;
   BfsDevState &s = g->tmpl;
   std::memset(&s, 0, sizeof(s));
   s.indptr = g->indptr;
   s.inds = g->inds;
+  s.nnz = (uint32_t)g->nnz;
+  s.inds_off = (uint32_t)((reinterpret_cast<uintptr_t>(g->inds) & 15u) >> 2);
   s.n_rows = g->n_rows;
   s.n_cols = g->n_cols;
   s.words = g->words;
@@ -134,7 +137,8 @@ static bfs_status setup_workspace(bfs_graph *g) {
   s.prev = (uint32_t *)p; p += bm;
   for (int b = 0; b < 2; b++) {
     s.qb[b] = (uint32_t *)p; p += q4;
-    s.qp[b] = (uint32_t *)p; p += qp4;
+    s.qd[b] = (uint32_t *)p; p += q4;
+    s.qc[b] = (uint32_t *)p; p += qp4;
     s.qv[b] = (uint32_t *)p; p += q4;
   }
   s.rec_frontier = (uint32_t *)p; p += rec;
@@ -165,6 +169,23 @@ static bfs_status setup_workspace(bfs_graph *g) {
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
                                                    kLevelgenBlock, 0));
   g->lg_grid = g->num_sms * std::max(occ_lg, 1);
+  // explore_any takes the hub prefix in dynamic shared memory, up to what
+  // the device allows a block beside the kernel's own static arrays
+  size_t static_max = 0;
+  for (int u = 0; u < 2; u++)
+    for (int par = 0; par < 2; par++) {
+      cudaFuncAttributes fa;
+      CK(cudaFuncGetAttributes(&fa, explore_any_kernel_fn(u ? 8 : 4, par != 0)));
+      static_max = std::max(static_max, fa.sharedSizeBytes);
+    }
+  g->hub_max = hub_max_vertices(g, static_max);
+  if (g->hub_max > 0) {
+    for (int u = 0; u < 2; u++)
+      for (int par = 0; par < 2; par++)
+        CK(cudaFuncSetAttribute(explore_any_kernel_fn(u ? 8 : 4, par != 0),
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(g->hub_max / 8)));
+  }
 
   // L2 access-policy window over the two visited bitmaps
   int max_persist = 0, max_window = 0;
@@ -302,9 +323,22 @@ static int host_blocks(const bfs_graph *g, int arm, int sm_factor, int ipt, uint
       1, std::min<uint64_t>(want, persistent_blocks(g, arm, sm_factor, ipt)));
 }
 
+// Dynamic shared memory of explore_any for the handle's current layout.
+static size_t hub_smem(const bfs_graph *g) {
+  return g->hub ? (size_t)g->hub->vertices / 8 : 0;
+}
+
 cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32_t F,
                            uint32_t EF, bool persistent) {
   BfsDevState *st = g->d_st;
+  if (arm_lb(arm) == BFS_LB_GLB) {
+    // GLB runs in explore_any (chunk walk, hub filter): one block per SM
+    void *aargs[] = {&st, &arm};
+    const int full = any_blocks(g, ipt);
+    const int grid = persistent ? full : std::min(full, host_blocks(g, arm, 0, ipt, F, EF));
+    return cudaLaunchKernel(explore_any_kernel_fn(ipt, g->run_parents), dim3(grid),
+                            dim3(kAnyBlock), aargs, hub_smem(g), g->stream);
+  }
   void *args[] = {&st};
   const int grid = persistent ? persistent_blocks(g, arm, sm_factor, ipt)
                               : host_blocks(g, arm, sm_factor, ipt, F, EF);
@@ -323,12 +357,13 @@ static void set_window(const bfs_graph *g, cudaGraphNode_t node) {
 
 static cudaError_t add_kernel(cudaGraph_t graph, cudaGraphNode_t *node,
                               const cudaGraphNode_t *deps, size_t ndeps, const void *fn,
-                              int grid, int block, void **args) {
+                              int grid, int block, void **args, size_t smem = 0) {
   cudaKernelNodeParams kp;
   std::memset(&kp, 0, sizeof(kp));
   kp.func = const_cast<void *>(fn);
   kp.gridDim = dim3(grid);
   kp.blockDim = dim3(block);
+  kp.sharedMemBytes = (unsigned)smem;
   kp.kernelParams = args;
   return cudaGraphAddKernelNode(node, graph, deps, ndeps, &kp);
 }
@@ -368,12 +403,14 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   cudaGraph_t body = wp.conditional.phGraph_out[0];
 
   void *ex_args[] = {&st};
-  if (arm >= 0) {
+  int arm_arg = arm;  // < 0: the scheduler's arm in st->arm
+  void *any_args[] = {&st, &arm_arg};
+  if (arm >= 0 && arm_lb(arm) != BFS_LB_GLB) {
     CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt, g->run_parents),
                   persistent_blocks(g, arm, sm_factor, ipt), arm_block(arm), ex_args));
   } else {
     CK(add_kernel(body, &n_explore, nullptr, 0, explore_any_kernel_fn(ipt, g->run_parents),
-                  any_blocks(g, ipt), kAnyBlock, ex_args));
+                  any_blocks(g, ipt), kAnyBlock, any_args, hub_smem(g)));
   }
   set_window(g, n_explore);
   void *lg_args[] = {&st, &cond_arg, &one};
@@ -469,6 +506,31 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, int ipt,
   return BFS_OK;
 }
 
+// The hub prefix size a request asks for on this handle (0: no layout).
+static uint32_t hub_target(const bfs_graph *g) {
+  if (g->hub_max == 0 || g->hub_request == 0) return 0;
+  uint64_t k = g->hub_request < 0 ? (uint64_t)kHubDefaultVertices : (uint64_t)g->hub_request;
+  k = std::min<uint64_t>(k, g->hub_max);
+  return (uint32_t)(k / 128u * 128u);
+}
+
+// Builds the hub layout the handle's request asks for, once; a build that
+// ran out of device memory is not retried until the request is made again.
+bfs_status ensure_hub(bfs_graph *g) {
+  const uint32_t want = hub_target(g);
+  if (g->hub_tried && g->hub_built_for == want) return BFS_OK;
+  g->hub_tried = true;
+  g->hub_built_for = want;
+  bfs_status rc = build_hub(g, want);
+  // cached loop graphs were built for the previous layout's launch shapes
+  for (auto &kv : g->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  g->graphs.clear();
+  return rc;
+}
+
 bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_in,
                            int32_t *levels_dev, int32_t *parents_dev, bfs_stats *stats,
                            LevelTimer *timer, const std::function<bfs_status()> *after_launch) {
@@ -509,12 +571,24 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     std::memset(stats->level_explore_ms, 0, sizeof(stats->level_explore_ms));
     std::memset(stats->level_gen_ms, 0, sizeof(stats->level_gen_ms));
   }
+  bfs_status hrc = ensure_hub(g);
+  if (hrc != BFS_OK) return hrc;
   BfsDevState &s = *g->h_st;
   s = g->tmpl;
   s.root = root;
   s.level = levels_dev;
   s.parent = parents_dev;
   s.fixed_arm = arm;
+  if (g->hub) {
+    s.indptr = g->hub->indptr;
+    s.inds = g->hub->inds;
+    s.inds_off = (uint32_t)((reinterpret_cast<uintptr_t>(g->hub->inds) & 15u) >> 2);
+    s.perm = g->hub->perm;
+    s.pinv = g->hub->pinv;
+    s.hub_words = g->hub->vertices / 32u;
+    s.hub_min_edges = g->hub_min_edges ? g->hub_min_edges
+                                       : std::max<uint32_t>(kHubMinEdges, 2u * g->hub->vertices);
+  }
   const bool graph_loop = o.loop == BFS_LOOP_GRAPH && !timer && o.record < 2;
   GraphEntry *ge = nullptr;
   bfs_status rc;
@@ -686,6 +760,7 @@ bfs_status bfs_graph_free(bfs_graph *g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   free_sched(g);
   free_msbfs(g);
+  free_hub(g);
   free_workspace(g);
   if (g->owns_csc) {
     cudaFree(g->indptr);
@@ -822,6 +897,29 @@ bfs_status bfs_validate_device(bfs_graph *g, uint32_t root, const int32_t *level
   cudaFree(d_bad);
   if (e != cudaSuccess) return fail(BFS_ERR_CUDA, std::string("validate: ") + cudaGetErrorString(e));
   *bad = h_bad;
+  return BFS_OK;
+}
+
+bfs_status bfs_hub_configure(bfs_graph *g, int64_t vertices, uint32_t min_edges) {
+  if (!g) return fail(BFS_ERR_INVALID_ARG, "null graph");
+  if (vertices < -1) return fail(BFS_ERR_INVALID_ARG, "hub vertices must be -1, 0 or positive");
+  CK(cudaSetDevice(g->device));
+  CK(cudaStreamSynchronize(g->stream));
+  g->hub_request = vertices;
+  g->hub_min_edges = min_edges;
+  g->hub_tried = false;  // an explicit request is built again, even after a failure
+  return ensure_hub(g);
+}
+
+bfs_status bfs_hub_info(bfs_graph *g, uint32_t *vertices, int32_t *relabelled,
+                        uint32_t *max_vertices) {
+  if (!g) return fail(BFS_ERR_INVALID_ARG, "null graph");
+  CK(cudaSetDevice(g->device));
+  bfs_status rc = ensure_hub(g);
+  if (rc != BFS_OK) return rc;
+  if (vertices) *vertices = g->hub ? g->hub->vertices : 0u;
+  if (relabelled) *relabelled = g->hub && g->hub->relabelled ? 1 : 0;
+  if (max_vertices) *max_vertices = g->hub_max;
   return BFS_OK;
 }
 

@@ -16,6 +16,7 @@ struct GraphEntry {
 };
 
 struct SchedModel;
+struct HubLayout;
 
 // Hooks of the host-driven level loop: `choose` picks the explore arm of a
 // level (learned scheduler, recorder), `before`/`after` bracket the explore
@@ -39,6 +40,14 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts,
 // loop) instead of a grid sized to the frontier.
 cudaError_t launch_explore(bfs_graph *g, int arm, int ipt, int sm_factor, uint32_t F,
                            uint32_t EF, bool persistent);
+// Builds the hub layout the handle's request asks for (once per request).
+bfs_status ensure_hub(bfs_graph *g);
+// Default hub prefix (vertices) and the smallest level (frontier edges) for
+// which the explore kernel loads it: a 32 KiB shared-memory bitmap (larger
+// prefixes take L1 capacity that the remaining bitmap probes need), loaded by
+// every block, pays off once the level has millions of edges.
+constexpr uint32_t kHubDefaultVertices = 1u << 18;
+constexpr uint32_t kHubMinEdges = 1u << 21;
 void free_sched(bfs_graph *g);   // bfs_sched.cu
 void free_msbfs(bfs_graph *g);   // msbfs.cu
 
@@ -83,4 +92,13 @@ struct bfs_graph {
   uint32_t host_launches = 0;
   bfsgb::SchedModel *sched = nullptr;
   MsWorkspace *ms = nullptr;  // multi-source BFS workspace (lazy)
+  // hub layout of the single-root path (hub_layout.cu), built on the first
+  // run that wants it; hub_request: -1 = automatic size, 0 = off, else the
+  // prefix size in vertices
+  bfsgb::HubLayout *hub = nullptr;
+  int64_t hub_request = -1;
+  uint32_t hub_max = 0;        // largest prefix the device's shared memory holds
+  uint32_t hub_min_edges = 0;  // level size from which explore loads it (0: automatic)
+  uint32_t hub_built_for = 0;  // the request the current layout was built for
+  bool hub_tried = false;
 };

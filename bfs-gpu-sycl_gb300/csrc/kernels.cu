@@ -41,18 +41,26 @@
 
 namespace bfsgb {
 
-// Test-then-claim of bit n.  The plain load may see a stale 0 (L1 copy);
-// atomicOr's return value is authoritative, so exactly one thread claims n.
-__device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent,
-                                      uint32_t from) {
+// Claim of bit n after a plain load saw it clear (the load may see a stale 0
+// from an L1 copy; atomicOr's return value is authoritative, so exactly one
+// thread claims n).  Parents are written in original ids (perm: internal ->
+// original, null for the identity); `from` already is one.
+__device__ __forceinline__ void claim(uint32_t *vis, uint32_t n, int32_t *parent, uint32_t from,
+                                      const uint32_t *perm) {
   const uint32_t w = n >> 5, bit = 1u << (n & 31u);
-  if (vis[w] & bit) return;
   if (parent) {
     const uint32_t old = atomicOr(vis + w, bit);
-    if (!(old & bit)) parent[n] = (int32_t)from;
+    if (!(old & bit)) parent[perm ? perm[n] : n] = (int32_t)from;
   } else {
     red_or(vis + w, bit);  // result unused: a reduction, no round trip
   }
+}
+
+// Test-then-claim of bit n.
+__device__ __forceinline__ void visit(uint32_t *vis, uint32_t n, int32_t *parent,
+                                      uint32_t from, const uint32_t *perm) {
+  if (vis[n >> 5] & (1u << (n & 31u))) return;
+  claim(vis, n, parent, from, perm);
 }
 
 // Owner resolution for one warp round.  `cur` is an entry whose start is at
@@ -146,28 +154,33 @@ __device__ __forceinline__ void stage_weights(float *dst, const float *__restric
 }
 
 __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_cond) {
-  const uint32_t r = st->root;
-  st->vis[r >> 5] |= 1u << (r & 31u);
-  st->prev[r >> 5] |= 1u << (r & 31u);
+  const uint32_t r = st->root;                     // original id
+  const uint32_t ri = st->pinv ? st->pinv[r] : r;  // internal id
+  st->vis[ri >> 5] |= 1u << (ri & 31u);
+  st->prev[ri >> 5] |= 1u << (ri & 31u);
   st->level[r] = 0;
   if (st->parent) st->parent[r] = (int32_t)r;
-  const bool expanded = r < st->n_rows;  // run_bfs_cpu.hpp:31
+  const bool expanded = ri < st->n_rows;  // run_bfs_cpu.hpp:31
   uint32_t b = 0, e = 0;
   if (expanded) {
-    b = st->indptr[r];
-    e = st->indptr[r + 1];
+    b = st->indptr[ri];
+    e = st->indptr[ri + 1];
   }
   if (expanded && e > b) {
+    const uint32_t nch = edge_chunks(b, e - b, st->inds_off);
     st->qb[0][0] = b;
-    st->qp[0][0] = 0;
-    st->qp[0][1] = e - b;
+    st->qd[0][0] = e - b;
+    st->qc[0][0] = 0;
+    st->qc[0][1] = nch;
     st->qv[0][0] = r;
     st->F = 1;
     st->EF = e - b;
+    st->EC = nch;
   } else {
-    st->qp[0][0] = 0;
+    st->qc[0][0] = 0;
     st->F = 0;
     st->EF = 0;
+    st->EC = 0;
   }
   st->edges_count = expanded ? (unsigned long long)(e - b) : 0ull;
   st->cur = 0;
@@ -176,6 +189,7 @@ __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_con
   st->reached_prev = 1;
   st->max_level = 0;
   st->next_packed = 0;
+  st->next_edges = 0;
   st->done_blocks = 0;
   st->lg_cursor = 0;
   st->error = 0;
@@ -237,11 +251,12 @@ __device__ __forceinline__ void explore_local_body(const BfsDevState *__restrict
   constexpr int NW = B / 32;
   const uint32_t cur_q = st->cur;
   const uint32_t *__restrict__ qb = st->qb[cur_q];
-  const uint32_t *__restrict__ qp = st->qp[cur_q];
+  const uint32_t *__restrict__ qd = st->qd[cur_q];
   const uint32_t *__restrict__ qv = st->qv[cur_q];
   const uint32_t *__restrict__ inds = st->inds;
   uint32_t *vis = st->vis;
   int32_t *parent = PAR ? st->parent : nullptr;
+  const uint32_t *perm = PAR ? st->perm : nullptr;
   const uint32_t lane = tid & 31u, warp = tid >> 5;
   const uint32_t num_tiles = (F + B - 1) / B;
   const uint64_t pol = evict_first_policy();
@@ -251,7 +266,7 @@ __device__ __forceinline__ void explore_local_body(const BfsDevState *__restrict
     uint32_t beg = 0, deg = 0, vid = 0;
     if (slot < F) {
       beg = qb[slot];
-      deg = qp[slot + 1] - qp[slot];
+      deg = qd[slot];
       if (PAR) vid = qv[slot];
     }
     const uint32_t incl = warp_incl_scan(deg, lane);
@@ -307,7 +322,7 @@ __device__ __forceinline__ void explore_local_body(const BfsDevState *__restrict
         for (int u = 0; u < U; u++) nb[u] = addr[u] != kFull ? ld_stream(inds + addr[u], pol) : 0u;
 #pragma unroll
         for (int u = 0; u < U; u++)
-          if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
+          if (addr[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u, perm);
       }
     }
     vblock_sync<B>(bar);
@@ -328,159 +343,235 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
                                          s_vid, s_wsum, 0u);
 }
 
-// ---- explore: GLB -----------------------------------------------------------
-// Edge-balanced: the frontier's edges [0, EF) are cut into equal warp chunks
-// dealt over the whole grid (run_bfs_gpu.hpp:318-366 deals single edges over
-// SMs*SM_FACTOR work-groups).  The grid-wide exclusive scan of degrees is the
-// queue's prefix array written by level generation (EN1-EN3, :203-307).
-// A warp finds the owner of its chunk start with a 32-ary search of the scan
-// (one probe per lane and round), then walks forward: each round loads the
-// next 32 entry starts and first-edge offsets coalesced, and every lane takes
-// its owner's offsets from those registers with shuffles.
-// GLB walk of one warp: global warp index gw out of total_warps.
-template <int U, bool PAR>
-__device__ __forceinline__ void explore_global_body(const BfsDevState *__restrict__ st,
-                                                    uint32_t F, uint32_t gw,
-                                                    uint32_t total_warps) {
+// ---- explore: GLB over 16-byte chunks of the edge array --------------------
+// Edge-balanced (run_bfs_gpu.hpp:318-366 deals single edges over
+// SMs * SM_FACTOR work-groups after a grid-wide scan of the frontier's
+// degrees, EN1-EN3 at :203-307).  Here the frontier's edges are walked in
+// chunk space: counting 16-byte chunks from the 16-byte boundary at or
+// below inds, an entry whose edges are inds[b, b + deg) owns the chunks
+// (b + off)/4 .. (b + off + deg - 1)/4 (off = st->inds_off), and the queue's
+// qc array, written by level generation, is the exclusive prefix of those
+// counts in queue order: the grid-wide scan.  The chunk space [0, EC) is cut
+// into equal warp chunks dealt over the grid; a warp finds the owner of its
+// first chunk with a 32-ary search of qc, then walks forward in rounds of
+// 32 chunks, one per lane: one 16-byte load and one owner resolution serve
+// four edge slots.  Owners are resolved with a warp OR-reduction of the next
+// 32 entry starts plus a popc (O(1) per chunk, instead of the reference's
+// per-edge binary search, :336-346).  The slots outside [b, b + deg) -- only
+// in an entry's first and last chunk -- are masked off, and a chunk that
+// reaches outside inds (the first one when off > 0, the last one when the
+// array does not fill it) is read with scalar loads of its valid slots
+// only.  U chunks per lane (4 U edge slots) are loaded per group, and the
+// next group's loads are issued before the current group's probes.
+//
+// HUB: probes of internal ids below hub_lim first test the block's
+// shared-memory copy s_hub of those bits of the visited bitmap (the hub
+// prefix under the hub layout); a set bit there means visited and no global
+// probe is made.  A clear one says nothing about claims made since by other
+// blocks, so the global test-then-claim follows, and a claimed hub's bit is
+// then set in s_hub for the block's later probes (bits only ever go from 0
+// to 1, so any snapshot is a valid "already visited" set).
+template <int U, bool PAR, bool HUB>
+__device__ __forceinline__ void explore_chunk_body(const BfsDevState *__restrict__ st,
+                                                   uint32_t F, uint32_t gw,
+                                                   uint32_t total_warps, uint32_t *s_hub,
+                                                   uint32_t hub_lim) {
   constexpr uint32_t kRound = 32u * U;
   constexpr uint32_t kMinChunk = kRound * kGlbGroups;
-  const uint32_t EF = st->EF;
+  const uint32_t EC = st->EC;
   const uint32_t cur_q = st->cur;
   const uint32_t *__restrict__ qb = st->qb[cur_q];
-  const uint32_t *__restrict__ qp = st->qp[cur_q];
+  const uint32_t *__restrict__ qd = st->qd[cur_q];
+  const uint32_t *__restrict__ qc = st->qc[cur_q];
   const uint32_t *__restrict__ qv = st->qv[cur_q];
-  const uint32_t *__restrict__ inds = st->inds;
+  const uint32_t off = st->inds_off;
+  // chunk k is bytes [16 k, 16 k + 16) from the boundary at or below inds
+  const uint32_t *__restrict__ inds0 = st->inds - off;
+  const uint4 *__restrict__ inds4 = reinterpret_cast<const uint4 *>(inds0);
+  // chunks lo4 .. hi4 - 1 lie wholly inside inds
+  const uint32_t lo4 = off ? 1u : 0u;
+  const uint32_t hi4 = (st->nnz + off) >> 2;
   uint32_t *vis = st->vis;
+  const uint32_t *vis_c = vis;  // plain loads of the visited words
   int32_t *parent = PAR ? st->parent : nullptr;
+  const uint32_t *perm = PAR ? st->perm : nullptr;
   const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t le_mask = (2u << lane) - 1u;  // lanes 0 .. lane (all for lane 31)
   const uint64_t pol = evict_first_policy();
-  // about four chunks per warp (each chunk costs one owner search), whole
-  // groups of U rounds, at least kMinChunk edges
-  uint64_t ch = ((uint64_t)EF + 4ull * total_warps - 1) / (4ull * total_warps);
+  // about four warp chunks per warp, whole groups of U rounds
+  uint64_t ch = ((uint64_t)EC + 4ull * total_warps - 1) / (4ull * total_warps);
   ch = (ch + kRound - 1) / kRound * kRound;
   const uint32_t CHUNK = (uint32_t)(ch > kMinChunk ? ch : kMinChunk);
-  const uint32_t n_chunks = (uint32_t)(((uint64_t)EF + CHUNK - 1) / CHUNK);
+  const uint32_t n_chunks = (uint32_t)(((uint64_t)EC + CHUNK - 1) / CHUNK);
 
   for (uint32_t c = gw; c < n_chunks; c += total_warps) {
-    const uint32_t w0 = c * CHUNK;  // < EF, no overflow
-    const uint32_t w1 = (uint32_t)min((uint64_t)EF, (uint64_t)w0 + CHUNK);
-    // An entry's edge e lives at inds[e + (qb - qp)]: one difference per
-    // entry (mod 2^32) instead of its start and first edge, so a lane needs
-    // one shuffle per round to address its edge.  Shuffles and warp
-    // reductions use the same L1 data pipe as the bitmap probes.
-    uint32_t cur = warp_owner_search(qp, F, w0, lane);
-    uint32_t cur_d = qb[cur] - qp[cur];
-    uint32_t cur_vid = PAR ? qv[cur] : 0u;
-    // Window: starts / differences / ids of entries c0 + 1 .. c0 + 32, one
-    // per lane.  It serves every round whose starts all lie inside it, i.e.
-    // while the start of entry c0 + 32 is >= the round's last edge; only
-    // then is it re-based at cur (about once per 32 entries, not per round).
-    uint32_t c0 = cur;
-    uint32_t bnd = (c0 + 1u + lane <= F) ? qp[c0 + 1u + lane] : kFull;  // qp[F] = EF
-    uint32_t dl = (c0 + 1u + lane < F) ? qb[c0 + 1u + lane] - bnd : 0u;
-    uint32_t vd = (PAR && c0 + 1u + lane < F) ? qv[c0 + 1u + lane] : 0u;
+    const uint32_t w0 = c * CHUNK;  // < EC
+    const uint32_t w1 = (uint32_t)min((uint64_t)EC, (uint64_t)w0 + CHUNK);
+    uint32_t cur = warp_owner_search(qc, F, w0, lane);
+    // the current owner: chunk offset (b >> 2) - qc (mod 2^32), edge range
+    // [cb, ce) counted from inds0 (edge p of inds is at p + off), vertex id
+    uint32_t cb = qb[cur] + off;
+    uint32_t ce = cb + qd[cur];
+    uint32_t cd = (cb >> 2) - qc[cur];
+    uint32_t cv = PAR ? qv[cur] : 0u;
+    // window: entries c0 + 1 .. c0 + 32, one per lane (chunk start, offset,
+    // edge range, id); re-based only when a round could leave it
+    uint32_t c0 = cur, bnd, wd, wb, we, wv;
+    auto load_window = [&]() {
+      const uint32_t j = c0 + 1u + lane;
+      bnd = (j <= F) ? qc[j] : kFull;  // qc[F] = EC
+      wb = we = wd = wv = 0u;
+      if (j < F) {
+        wb = qb[j] + off;
+        we = wb + qd[j];
+        wd = (wb >> 2) - bnd;
+        if (PAR) wv = qv[j];
+      }
+    };
+    load_window();
     uint32_t wlast = __shfl_sync(kFull, bnd, 31);
-    // Edge addresses of the U rounds starting at edge `base`.
-    auto resolve = [&](uint32_t base, uint32_t (&ad)[U], uint32_t (&fr)[U]) {
+    // Resolves the U rounds of chunks starting at chunk `base` and issues
+    // their 16-byte loads: q (slots), m (valid-slot mask, bit i = slot i),
+    // fr (source id, with parents).
+    auto resolve = [&](uint32_t base, uint4 (&q)[U], uint32_t (&m)[U], uint32_t (&fr)[U]) {
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const uint32_t rb = base + 32u * u;
-        const uint32_t e = rb + lane;
+        const uint32_t x = rb + lane;
         if (wlast < rb || wlast - rb < 31u) {  // warp-uniform
           c0 = cur;
-          const uint32_t j = c0 + 1u + lane;
-          bnd = (j <= F) ? qp[j] : kFull;
-          dl = (j < F) ? qb[j] - bnd : 0u;
-          vd = (PAR && j < F) ? qv[j] : 0u;
+          load_window();
           wlast = __shfl_sync(kFull, bnd, 31);
         }
-        // entries at or before cur have starts < rb: p wraps past 32
-        const uint32_t p = bnd - rb;
-        const uint32_t starts = __reduce_or_sync(kFull, (p < 32u) ? (1u << p) : 0u);
-        const uint32_t k = __popc(starts & ((2u << lane) - 1u));
-        // entry cur + k sits in lane cur + k - c0 - 1 of the window
+        // entries at or before cur start before rb: their p wraps past 32
+        const uint32_t starts = __reduce_or_sync(kFull, bit_or_zero(bnd - rb));
+        const uint32_t k = __popc(starts & le_mask);
         const uint32_t srcl = k ? cur + k - c0 - 1u : 0u;
-        const uint32_t s_d = __shfl_sync(kFull, dl, srcl);
-        const uint32_t s_vid = PAR ? __shfl_sync(kFull, vd, srcl) : 0u;
-        ad[u] = kFull;
-        fr[u] = 0;
-        if (e < w1) {
-          ad[u] = e + (k ? s_d : cur_d);
-          if (PAR) fr[u] = k ? s_vid : cur_vid;
+        const uint32_t sd = __shfl_sync(kFull, wd, srcl);
+        const uint32_t sb = __shfl_sync(kFull, wb, srcl);
+        const uint32_t se = __shfl_sync(kFull, we, srcl);
+        const uint32_t sv = PAR ? __shfl_sync(kFull, wv, srcl) : 0u;
+        const uint32_t d = k ? sd : cd, b = k ? sb : cb, e = k ? se : ce;
+        fr[u] = PAR ? (k ? sv : cv) : 0u;
+        m[u] = 0u;
+        q[u] = make_uint4(0u, 0u, 0u, 0u);
+        if (x < w1) {
+          const uint32_t a4 = x + d;    // chunk index from inds0
+          const uint32_t p0 = a4 << 2;  // position of its slot 0
+          const uint32_t lo = b > p0 ? b - p0 : 0u;        // 0 .. 3
+          const uint32_t hi = e - p0 < 4u ? e - p0 : 4u;   // 1 .. 4
+          m[u] = (0xFu >> (4u - hi)) & (0xFu << lo);
+          if (a4 >= lo4 && a4 < hi4) {
+            q[u] = ld_stream4(inds4 + a4, pol);
+          } else {  // a chunk that reaches outside inds: its valid slots only
+            uint32_t t[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              if ((m[u] >> i) & 1u) t[i] = ld_stream(inds0 + p0 + i, pol);
+            q[u] = make_uint4(t[0], t[1], t[2], t[3]);
+          }
         }
         // the owner of lane 31 is entry cur + popc(starts)
         const uint32_t k31 = __popc(starts);
         if (k31) {
           cur += k31;
-          cur_d = __shfl_sync(kFull, dl, cur - c0 - 1u);
-          if (PAR) cur_vid = __shfl_sync(kFull, vd, cur - c0 - 1u);
+          const uint32_t sl = cur - c0 - 1u;
+          cd = __shfl_sync(kFull, wd, sl);
+          cb = __shfl_sync(kFull, wb, sl);
+          ce = __shfl_sync(kFull, we, sl);
+          if (PAR) cv = __shfl_sync(kFull, wv, sl);
         }
       }
     };
-    // Software pipeline: the edge loads of the next U rounds are issued
-    // before the bitmap probes of the current ones, so the probes' latency
-    // covers them.
-    uint32_t nb[U], from[U];
-    {
-      uint32_t ad[U];
-      resolve(w0, ad, from);
+    // Probes of the U chunks of a lane, in two phases: every slot's visited
+    // word is loaded (or, for an invalid slot or a hub the block already
+    // knows visited, replaced by its own bit) before any claim is issued --
+    // a claim is an asm statement that orders memory, so a load after it
+    // could not start before it.
+    auto probe = [&](const uint4 (&q)[U], const uint32_t (&m)[U], const uint32_t (&fr)[U]) {
+      uint32_t word[U][4];
 #pragma unroll
-      for (int u = 0; u < U; u++) nb[u] = ad[u] != kFull ? ld_stream(inds + ad[u], pol) : kFull;
-    }
-    for (uint32_t base = w0; base < w1; base += kRound) {
-      uint32_t nb2[U], from2[U];
-      if (base + kRound < w1) {  // warp-uniform; no overflow: w1 <= EF < 2^32 - kRound
-        uint32_t ad[U];
-        resolve(base + kRound, ad, from2);
+      for (int u = 0; u < U; u++) {
+        const uint32_t n4[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
 #pragma unroll
-        for (int u = 0; u < U; u++)
-          nb2[u] = ad[u] != kFull ? ld_stream(inds + ad[u], pol) : kFull;
-      } else {
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          nb2[u] = kFull;
-          from2[u] = 0;
+        for (int i = 0; i < 4; i++) {
+          const uint32_t n = n4[i];
+          const uint32_t bit = 1u << (n & 31u);
+          bool known = !((m[u] >> i) & 1u);
+          if (HUB && !known && n < hub_lim) known = (s_hub[n >> 5] & bit) != 0u;
+          word[u][i] = known ? bit : vis_c[n >> 5];
         }
       }
 #pragma unroll
-      for (int u = 0; u < U; u++)
-        if (nb[u] != kFull) visit(vis, nb[u], parent, PAR ? from[u] : 0u);
+      for (int u = 0; u < U; u++) {
+        const uint32_t n4[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t n = n4[i];
+          const uint32_t bit = 1u << (n & 31u);
+          if (word[u][i] & bit) continue;
+          claim(vis, n, parent, fr[u], perm);
+          if (HUB && n < hub_lim) atomicOr(s_hub + (n >> 5), bit);
+        }
+      }
+    };
+    // Software pipeline: the loads of the next U rounds are issued before
+    // the probes of the current ones, so that they overlap.
+    uint4 q[U], q2[U];
+    uint32_t m[U], m2[U], fr[U], fr2[U];
+    resolve(w0, q, m, fr);
+    for (uint32_t base = w0; base < w1; base += kRound) {
+      const bool more = base + kRound < w1;  // warp-uniform; no overflow: w1 < 2^32 - kRound
+      if (more) resolve(base + kRound, q2, m2, fr2);
+      probe(q, m, fr);
+      if (!more) break;
 #pragma unroll
       for (int u = 0; u < U; u++) {
-        nb[u] = nb2[u];
-        from[u] = from2[u];
+        q[u] = q2[u];
+        m[u] = m2[u];
+        fr[u] = fr2[u];
       }
     }
   }
 }
 
+// The GLB arms' own kernel (the engine runs GLB levels in explore_any; the
+// allocation-free entry point launches this one): 1024 threads per SM,
+// ipt / 2 chunks per lane and group.
 template <int B, int U, bool PAR>
-__global__ void __launch_bounds__(B, (MinBlocks<B, U, true>::value))
+__global__ void __launch_bounds__(B, 1024 / B)
     explore_global_kernel(BfsDevState *__restrict__ st) {
   const uint32_t F = st->F;
   if (F == 0) return;
   note_arm<1 * 3 + BlockIndex<B>::value>(st);
-  explore_global_body<U, PAR>(st, F, blockIdx.x * (B / 32) + (threadIdx.x >> 5),
-                              gridDim.x * (B / 32));
+  explore_chunk_body<U / 2, PAR, false>(st, F, blockIdx.x * (B / 32) + (threadIdx.x >> 5),
+                                        gridDim.x * (B / 32), nullptr, 0u);
 }
 
 // ---- explore: any arm, chosen on the device ---------------------------------
-// One 512-thread kernel for the learned schedule in the CUDA-graph loop: it
-// runs the arm the scheduler stored in st->arm (init or the last block of the
-// previous level generation picked it), so the loop needs no switch node.
-// GLB does not depend on the block size (edges are dealt per warp over the
-// grid); LLB / SLB tiles of 128 or 256 entries run on 4 or 2 slices of the
-// block, each with its own shared arrays and named barrier.
+// One kAnyBlock-thread kernel, one block per SM, that runs any arm: the arm
+// passed in (arm_in >= 0; the GLB arms always run here, and so does every
+// arm the per-level recorder times) or, with arm_in < 0, the arm the learned
+// scheduler stored in st->arm (init or the last block of the previous level
+// generation picked it), so the learned loop needs no switch node.
+//   GLB  the 16-byte chunk walk, chunks dealt per warp over the grid (the
+//        block size of the arm does not matter), ipt / 2 chunks per lane and
+//        group.  With a hub layout, levels of at least hub_min_edges edges
+//        first copy the hub prefix of the visited bitmap into the block's
+//        dynamic shared memory (s_hub) and probe through it.
+//   LLB / SLB  tiles of 128, 256 or 512 entries on 8, 4 or 2 slices of the
+//        block, each with its own shared arrays and named barrier.
 template <int U, bool PAR>
-__global__ void __launch_bounds__(kAnyBlock, (U <= 4 ? 2048 : 1024) / kAnyBlock)
-    explore_any_kernel(BfsDevState *__restrict__ st) {
-  __shared__ uint32_t s_off[kAnyBlock + 4];
+__global__ void __launch_bounds__(kAnyBlock, 1)
+    explore_any_kernel(BfsDevState *__restrict__ st, int arm_in) {
+  extern __shared__ __align__(16) uint32_t s_hub[];
+  __shared__ uint32_t s_off[kAnyBlock + 8];
   __shared__ uint32_t s_dif[kAnyBlock];
   __shared__ uint32_t s_vid[kAnyBlock];
   __shared__ uint32_t s_wsum[kAnyBlock / 32];
   const uint32_t F = st->F;
   if (F == 0) return;
-  const int arm = st->arm;  // uniform over the grid
+  const int arm = arm_in >= 0 ? arm_in : st->arm;  // uniform over the grid
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const uint32_t l = st->lvl;
     if (l < st->rec_cap) st->rec_ran[l] = arm;
@@ -488,33 +579,45 @@ __global__ void __launch_bounds__(kAnyBlock, (U <= 4 ? 2048 : 1024) / kAnyBlock)
   const int form = arm / 3, bi = arm % 3;
   const uint32_t t = threadIdx.x;
   if (form == BFS_LB_GLB) {
-    explore_global_body<U, PAR>(st, F, blockIdx.x * (kAnyBlock / 32) + (t >> 5),
-                                gridDim.x * (kAnyBlock / 32));
+    const uint32_t hw = st->hub_words;  // a multiple of 4
+    const bool use = hw != 0 && st->EF >= st->hub_min_edges;  // uniform over the grid
+    if (use) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(st->vis);
+      uint4 *dst = reinterpret_cast<uint4 *>(s_hub);
+      for (uint32_t i = t; i < (hw >> 2); i += kAnyBlock) dst[i] = src[i];
+      __syncthreads();
+    }
+    explore_chunk_body<U / 2, PAR, true>(st, F, blockIdx.x * (kAnyBlock / 32) + (t >> 5),
+                                         gridDim.x * (kAnyBlock / 32), s_hub,
+                                         use ? hw * 32u : 0u);
   } else if (bi == 2) {
+    const uint32_t v = t >> 9, o = v * 513u;
     if (form == BFS_LB_SLB)
-      explore_local_body<512, true, U, PAR>(st, F, t, blockIdx.x, gridDim.x, s_off, s_dif, s_vid,
-                                            s_wsum, 1u);
+      explore_local_body<512, true, U, PAR>(st, F, t & 511u, blockIdx.x * 2 + v, gridDim.x * 2,
+                                            s_off + o, s_dif + v * 512, s_vid + v * 512,
+                                            s_wsum + v * 16, 1u + v);
     else
-      explore_local_body<512, false, U, PAR>(st, F, t, blockIdx.x, gridDim.x, s_off, s_dif,
-                                             s_vid, s_wsum, 1u);
+      explore_local_body<512, false, U, PAR>(st, F, t & 511u, blockIdx.x * 2 + v, gridDim.x * 2,
+                                             s_off + o, s_dif + v * 512, s_vid + v * 512,
+                                             s_wsum + v * 16, 1u + v);
   } else if (bi == 1) {
     const uint32_t v = t >> 8, o = v * 257u;
     if (form == BFS_LB_SLB)
-      explore_local_body<256, true, U, PAR>(st, F, t & 255u, blockIdx.x * 2 + v, gridDim.x * 2,
+      explore_local_body<256, true, U, PAR>(st, F, t & 255u, blockIdx.x * 4 + v, gridDim.x * 4,
                                             s_off + o, s_dif + v * 256, s_vid + v * 256,
                                             s_wsum + v * 8, 1u + v);
     else
-      explore_local_body<256, false, U, PAR>(st, F, t & 255u, blockIdx.x * 2 + v, gridDim.x * 2,
+      explore_local_body<256, false, U, PAR>(st, F, t & 255u, blockIdx.x * 4 + v, gridDim.x * 4,
                                              s_off + o, s_dif + v * 256, s_vid + v * 256,
                                              s_wsum + v * 8, 1u + v);
   } else {
     const uint32_t v = t >> 7, o = v * 129u;
     if (form == BFS_LB_SLB)
-      explore_local_body<128, true, U, PAR>(st, F, t & 127u, blockIdx.x * 4 + v, gridDim.x * 4,
+      explore_local_body<128, true, U, PAR>(st, F, t & 127u, blockIdx.x * 8 + v, gridDim.x * 8,
                                             s_off + o, s_dif + v * 128, s_vid + v * 128,
                                             s_wsum + v * 4, 1u + v);
     else
-      explore_local_body<128, false, U, PAR>(st, F, t & 127u, blockIdx.x * 4 + v, gridDim.x * 4,
+      explore_local_body<128, false, U, PAR>(st, F, t & 127u, blockIdx.x * 8 + v, gridDim.x * 8,
                                              s_off + o, s_dif + v * 128, s_vid + v * 128,
                                              s_wsum + v * 4, 1u + v);
   }
@@ -524,19 +627,22 @@ __global__ void __launch_bounds__(kAnyBlock, (U <= 4 ? 2048 : 1024) / kAnyBlock)
 __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_cond) {
   const unsigned long long packed = *(volatile unsigned long long *)&st->next_packed;
   const uint32_t f_new = (uint32_t)(packed >> 32);
-  const uint32_t ef_new = (uint32_t)packed;
+  const uint32_t ec_new = (uint32_t)packed;
+  const uint32_t ef_new = *(volatile uint32_t *)&st->next_edges;
   const uint32_t lvl = st->lvl + 1;
   const uint32_t reached = *(volatile uint32_t *)&st->reached;
   if (reached > st->reached_prev) st->max_level = lvl;
   st->reached_prev = reached;
   st->edges_count += ef_new;
   const uint32_t nq = st->cur ^ 1u;
-  st->qp[nq][f_new] = ef_new;  // trailing total of the new queue's scan
+  st->qc[nq][f_new] = ec_new;  // trailing total of the new queue's scan
   st->cur = nq;
   st->F = f_new;
   st->EF = ef_new;
+  st->EC = ec_new;
   st->lvl = lvl;
   st->next_packed = 0;
+  st->next_edges = 0;
   st->done_blocks = 0;
   st->lg_cursor = 0;
   st->launches += 2;
@@ -558,10 +664,13 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
 // its group's new vertices (vis & ~prev) in shared memory -- each lane walks
 // its word's set bits -- so that lane l of round r then takes the
 // (32 r + l)-th new vertex with one shared load, and 32 indptr loads are in
-// flight per round whatever the bit layout.  Pass 1 writes levels and counts
-// kept entries and their degrees; thread 0 reserves the block's queue slots
-// and edge offsets with one atomic and claims the block's next span in the
-// same step; pass 2 re-reads the (now cached) indptr pairs and writes the
+// flight per round whatever the bit layout.  Pass 1 writes levels (in
+// original ids under the hub layout) and counts kept entries, their degrees
+// and their 16-byte chunks; thread 0 reserves the block's queue slots and
+// chunk offsets with one atomic -- slots and the chunk prefix must come from
+// the same atomic, so that the prefix is in slot order -- adds the degrees
+// to the level's edge total and claims the block's next span in the same
+// step; pass 2 re-reads the (now cached) indptr pairs and writes the
 // entries.  Two block barriers per span.
 constexpr int kLgUnroll = 4;
 constexpr int kLgMinBlocks = 5;  // 1280 threads per SM: at most 48 registers
@@ -575,6 +684,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   static_assert(kSchedParams <= NW * 32 * 32, "the model must fit the list buffer");
   __shared__ uint32_t s_list[NW][32 * 32];
   __shared__ unsigned long long s_wtot[NW];
+  __shared__ uint32_t s_wdeg[NW];
   __shared__ unsigned long long s_base;
   __shared__ uint32_t s_sb[2];
   __shared__ uint32_t s_reached[NW];
@@ -589,8 +699,12 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   int32_t *__restrict__ level = st->level;
   const uint32_t nq = st->cur ^ 1u;
   uint32_t *__restrict__ qb = st->qb[nq];
-  uint32_t *__restrict__ qp = st->qp[nq];
+  uint32_t *__restrict__ qd = st->qd[nq];
+  uint32_t *__restrict__ qc = st->qc[nq];
   uint32_t *__restrict__ qv = st->qv[nq];
+  const uint32_t off = st->inds_off;
+  const uint32_t *__restrict__ perm = st->perm;  // internal -> original (null: identity)
+  const bool want_vid = st->parent != nullptr;   // vertex ids are read for parents only
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t *__restrict__ list = s_list[warp];
@@ -620,9 +734,10 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       __syncwarp();
     }
     reached += tot;
-    // pass 1: levels; kept-entry count and degree sum of the warp.  kLgUnroll
-    // rounds are resolved first so their indptr loads are in flight together.
-    uint32_t w_cnt = 0, w_deg = 0;
+    // pass 1: levels; kept-entry count, degree and chunk sums of the warp.
+    // kLgUnroll rounds are resolved first so their indptr loads are in flight
+    // together.
+    uint32_t w_cnt = 0, w_deg = 0, w_chk = 0;
     for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
       uint32_t b[kLgUnroll], e[kLgUnroll];
 #pragma unroll
@@ -631,7 +746,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
         b[r] = e[r] = 0;
         if (t < tot) {
           const uint32_t v = list[t];
-          level[v] = lvl_next;
+          level[perm ? perm[v] : v] = lvl_next;
           if (v < n_rows) {
             b[r] = indptr[v];
             e[r] = indptr[v + 1];
@@ -643,25 +758,32 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
         const uint32_t deg = e[r] - b[r];
         w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
         w_deg += __reduce_add_sync(kFull, deg);
+        w_chk += __reduce_add_sync(kFull, edge_chunks(b[r], deg, off));
       }
     }
     // block-wide offsets (one atomic per block and step) and the next span
-    if (lane == 0) s_wtot[warp] = ((unsigned long long)w_cnt << 32) | w_deg;
+    if (lane == 0) {
+      s_wtot[warp] = ((unsigned long long)w_cnt << 32) | w_chk;
+      s_wdeg[warp] = w_deg;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned long long run = 0;
+      uint32_t deg_sum = 0;
       for (int i = 0; i < NW; i++) {
         const unsigned long long x = s_wtot[i];
         s_wtot[i] = run;
         run += x;
+        deg_sum += s_wdeg[i];
       }
       s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
+      if (deg_sum) atomicAdd(&st->next_edges, deg_sum);  // a total: order does not matter
       s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
     }
     __syncthreads();
     if (w_cnt) {
       const unsigned long long wb = s_base + s_wtot[warp];
-      uint32_t slot = (uint32_t)(wb >> 32), pref = (uint32_t)wb;
+      uint32_t slot = (uint32_t)(wb >> 32), prefc = (uint32_t)wb;
       // pass 2: write the kept entries in the same order
       for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
         uint32_t vv[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
@@ -678,16 +800,18 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
 #pragma unroll
         for (int r = 0; r < kLgUnroll; r++) {
           const uint32_t deg = e[r] - b[r];
+          const uint32_t nch = edge_chunks(b[r], deg, off);
           const uint32_t km = __ballot_sync(kFull, deg > 0u);
-          const uint32_t dincl = warp_incl_scan(deg, lane);
+          const uint32_t cincl = warp_incl_scan(nch, lane);
           if (deg) {
             const uint32_t sl = slot + __popc(km & lt_mask);
             qb[sl] = b[r];
-            qp[sl] = pref + dincl - deg;
-            qv[sl] = vv[r];
+            qd[sl] = deg;
+            qc[sl] = prefc + cincl - nch;
+            if (want_vid) qv[sl] = perm ? perm[vv[r]] : vv[r];
           }
           slot += __popc(km);
-          pref += __shfl_sync(kFull, dincl, 31);
+          prefc += __shfl_sync(kFull, cincl, 31);
         }
       }
     }

@@ -8,8 +8,9 @@
 namespace bfsgb {
 
 constexpr int kLevelgenBlock = 256;
-// Block size of the explore kernel that runs any arm (learned schedule).
-constexpr int kAnyBlock = 512;
+// Block size of the explore kernel that runs any arm (learned schedule and
+// every GLB launch); one block per SM.
+constexpr int kAnyBlock = 1024;
 // Explore kernels keep U warp rounds (U edges per lane) in flight; U is the
 // "items per thread" tunable (4 or 8).  A GLB warp chunk is at least
 // kGlbGroups groups of U rounds (more when the level is large: about four
@@ -22,7 +23,10 @@ inline uint32_t glb_chunk_edges(int ipt) { return 32u * (uint32_t)ipt * kGlbGrou
 // (unsigned long long conditional_handle, int use_conditional).
 // parents: the variant that also records BFS-tree parents.
 const void *explore_kernel_fn(int arm, int ipt, bool parents);
-// The explore kernel that runs the arm stored in st->arm (kAnyBlock threads).
+// The explore kernel that runs any arm: arguments (BfsDevState*, int arm),
+// arm < 0 = the arm stored in st->arm; kAnyBlock threads, one block per SM,
+// dynamic shared memory of st->hub_words words for GLB levels behind the hub
+// filter (the function's maximum dynamic shared memory must be raised first).
 const void *explore_any_kernel_fn(int ipt, bool parents);
 const void *levelgen_kernel_fn();
 const void *init_kernel_fn();

@@ -8,7 +8,7 @@
 // memory it already owns), and the BFS workspace -- visited bitmaps, the two
 // frontier queues and the level-loop state -- lives in the file-scope device
 // array below.  It is sized for graphs of at most BFS_NOALLOC_MAX_VERTICES
-// vertices (about 24 MiB), and every GPU that loads this library keeps it
+// vertices (about 32 MiB), and every GPU that loads this library keeps it
 // until the process exits.
 //
 // Set-up: the first call on a device, with that device current, looks up the
@@ -61,7 +61,7 @@ constexpr size_t kPrevOff = kVisOff + align256(kWordsMax * 4);
 constexpr size_t kQ4 = align256((size_t)kMaxV * 4);
 constexpr size_t kQp4 = align256(((size_t)kMaxV + 1) * 4);
 constexpr size_t kQOff = kPrevOff + align256(kWordsMax * 4);
-constexpr size_t kScratchBytes = kQOff + 2 * (2 * kQ4 + kQp4);
+constexpr size_t kScratchBytes = kQOff + 2 * (3 * kQ4 + kQp4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -145,6 +145,8 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
   std::memset(&h, 0, sizeof(h));
   h.indptr = d_indptr;
   h.inds = d_inds;
+  h.nnz = (uint32_t)nnz;
+  h.inds_off = (uint32_t)((reinterpret_cast<uintptr_t>(d_inds) & 15u) >> 2);
   h.n_rows = n_rows;
   h.n_cols = n_cols;
   h.words = (uint32_t)((((size_t)n_cols + 31) / 32 + 31) / 32 * 32);
@@ -152,10 +154,11 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
   h.vis = (uint32_t *)(base + kVisOff);
   h.prev = (uint32_t *)(base + kPrevOff);
   for (int b = 0; b < 2; b++) {
-    unsigned char *q = base + kQOff + (size_t)b * (2 * kQ4 + kQp4);
+    unsigned char *q = base + kQOff + (size_t)b * (3 * kQ4 + kQp4);
     h.qb[b] = (uint32_t *)q;
-    h.qp[b] = (uint32_t *)(q + kQ4);
-    h.qv[b] = (uint32_t *)(q + kQ4 + kQp4);
+    h.qd[b] = (uint32_t *)(q + kQ4);
+    h.qc[b] = (uint32_t *)(q + 2 * kQ4);
+    h.qv[b] = (uint32_t *)(q + 2 * kQ4 + kQp4);
   }
   h.level = levels_dev;
   h.parent = nullptr;

@@ -130,6 +130,29 @@ bfs_status bfs_graph_info(const bfs_graph *g, uint32_t *n_rows, uint32_t *n_cols
 bfs_status bfs_graph_device_csc(const bfs_graph *g, const uint32_t **d_indptr,
                                 const uint32_t **d_inds);
 
+/* ---- hub layout of the single-root path -------------------------------- */
+/* No counterpart in the reference.  On power-law graphs most edges of the
+ * large levels point at a few high in-degree vertices reached levels
+ * earlier; the GLB explore kernel answers those visited-bitmap probes from
+ * shared memory.  For that the handle keeps a relabelled copy of the graph
+ * whose internal ids 0 .. K-1 are its K highest in-degree vertices (graphs
+ * of at most K vertices, and graphs with n_rows < n_cols, keep their own ids
+ * and no copy).  Levels, parents and every other entry point still use the
+ * caller's ids; results are identical with or without the layout.  The copy
+ * costs nnz + 3 n_cols + 1 uint32 of device memory; if it cannot be
+ * allocated the handle runs without it.
+ * vertices: -1 = automatic (the default: K = 2^18, capped by the device's
+ * shared memory), 0 = off, > 0 = K (rounded down to a multiple of 128).
+ * min_edges: the smallest level (frontier edges) for which the explore
+ * kernel loads the prefix into shared memory; 0 = automatic (max(2^21, 2K)).
+ * The layout is built by this call, or by the first single-root run. */
+bfs_status bfs_hub_configure(bfs_graph *g, int64_t vertices, uint32_t min_edges);
+/* The current layout: *vertices = K (0: none), *relabelled = 1 if the
+ * handle holds a relabelled copy, *max_vertices = the largest K the device
+ * allows.  Any output may be NULL. */
+bfs_status bfs_hub_info(bfs_graph *g, uint32_t *vertices, int32_t *relabelled,
+                        uint32_t *max_vertices);
+
 /* ---- single-root BFS -------------------------------------------------- */
 /* One BFS from root.  levels_host (n_cols int32, required) and parents_host
  * (n_cols int32, optional: parent of each reached vertex, the root is its own
@@ -249,7 +272,7 @@ int32_t bfs_multi_num_configs(int32_t *blocks, int32_t *ipts, int32_t *clusters,
  * One BFS from root over a CSC graph already on the current device, into
  * levels_dev (n_cols int32, caller-owned); *edges_count_out (optional, host)
  * receives the reference's edgesCount.  The workspace is a fixed device array
- * inside the library (about 24 MiB per GPU that loads it, held until exit),
+ * inside the library (about 32 MiB per GPU that loads it, held until exit),
  * so graphs are limited to BFS_NOALLOC_MAX_VERTICES vertices and larger ones
  * are rejected with BFS_ERR_INVALID_ARG.  The first call on a device looks
  * up that array's address (make it before any stream capture), and under

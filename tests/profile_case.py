@@ -6,12 +6,14 @@ Each case builds its input on the device from a fixed seed, runs the path once
 and prints what it ran, so that an ncu capture (`-k <kernel> -s <skip> -c <n>`)
 sees a known sequence of launches:
 
-  bfs SCALE ARM   R-MAT SCALE/EF16 seed 5, one BFS from the first seeded root
+  bfs SCALE ARM [HUB]
+                  R-MAT SCALE/EF16 seed 5, one BFS from the first seeded root
                   with the host-driven level loop (every level is a separate
                   launch, which ncu can capture; kernels inside a graph with a
                   conditional node cannot be).  ARM is llb|glb|slb followed by
-                  the block size, e.g. glb256.  Prints (level, frontier
-                  entries, edges) per level.
+                  the block size, e.g. glb256.  HUB: the hub layout's prefix
+                  size (0 = off; default: automatic).  Prints (level,
+                  frontier entries, edges) per level.
   batch SCALE     R-MAT SCALE/EF16 seed 6, one 64-root multi-source pass
                   (host-driven level loop, as above).
   multi [B I C]   the 256-graph mixed batch of the benchmark, one launch of
@@ -34,8 +36,9 @@ import torch  # noqa: E402
 import bfs_gb300 as B  # noqa: E402
 
 
-def case_bfs(scale, arm):
+def case_bfs(scale, arm, hub=-1):
     dg = B.Graph.gen_rmat_device(scale, 16, seed=5)
+    dg.hub_configure(hub)
     r = int(B.sample_roots(dg.download(), 1, 5)[0])
     lv = torch.empty(dg.n_cols, dtype=torch.int32, device="cuda")
     st = dg.run_device(r, lv.data_ptr(),
@@ -67,8 +70,8 @@ def main(argv):
         print(__doc__)
         return 2
     torch.cuda.set_device(0)
-    if argv[0] == "bfs" and len(argv) == 3:
-        case_bfs(int(argv[1]), argv[2])
+    if argv[0] == "bfs" and len(argv) in (3, 4):
+        case_bfs(int(argv[1]), argv[2], *(int(x) for x in argv[3:]))
     elif argv[0] == "batch" and len(argv) == 2:
         case_batch(int(argv[1]))
     elif argv[0] == "multi" and len(argv) in (1, 4):

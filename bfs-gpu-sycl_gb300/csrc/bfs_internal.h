@@ -112,6 +112,7 @@ struct BfsDevState {
   // parents are written in original ids.  Null: identity.
   const uint32_t *perm;  // internal id -> original id
   const uint32_t *pinv;  // original id -> internal id
+  const uint32_t *moved; // bitmap: bit v set when perm[v] != v (null: identity)
   uint32_t hub_words;    // bitmap words of the hub prefix kept in shared memory
   uint32_t hub_min_edges;  // frontier edges from which explore loads them
   // level-loop counters (written by kernels)

@@ -33,6 +33,21 @@ __device__ __forceinline__ uint32_t bit_or_zero(uint32_t p) {
   asm("shl.b32 %0, 1, %1;" : "=r"(r) : "r"(p));
   return r;
 }
+// Loads *p into r only when pred != 0 (a predicated load: no branch, and no
+// memory request for lanes whose predicate is off); r keeps its value
+// otherwise.  Not volatile and without a memory clobber, so the compiler may
+// move it freely -- used for visited-bitmap words, where a stale value only
+// costs an extra claim (bits only ever go from 0 to 1).
+__device__ __forceinline__ void ld_global_if(uint32_t &r, const uint32_t *p, uint32_t pred) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.u32 %0, [%1];\n\t}"
+      : "+r"(r)
+      : "l"(p), "r"(pred));
+}
+__device__ __forceinline__ void ld_shared_if(uint32_t &r, uint32_t saddr, uint32_t pred) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.shared.u32 %0, [%1];\n\t}"
+      : "+r"(r)
+      : "r"(saddr), "r"(pred));
+}
 // Fire-and-forget OR into global memory (a reduction: no value comes back,
 // so nothing is written back to the registers of the issuing warp).
 __device__ __forceinline__ void red_or(uint32_t *p, uint32_t v) {

@@ -585,6 +585,7 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     s.inds_off = (uint32_t)((reinterpret_cast<uintptr_t>(g->hub->inds) & 15u) >> 2);
     s.perm = g->hub->perm;
     s.pinv = g->hub->pinv;
+    s.moved = g->hub->moved;
     s.hub_words = g->hub->vertices / 32u;
     s.hub_min_edges = g->hub_min_edges ? g->hub_min_edges
                                        : std::max<uint32_t>(kHubMinEdges, 2u * g->hub->vertices);

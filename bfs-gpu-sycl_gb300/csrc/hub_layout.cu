@@ -102,6 +102,16 @@ __global__ void finish_pinv_kernel(uint32_t n, uint32_t *pinv, const uint32_t *_
   }
 }
 
+// Bit v of `moved` is set when perm[v] != v (one ballot per 32 vertices).
+__global__ void moved_kernel(const uint32_t *__restrict__ perm, uint32_t n, uint32_t words,
+                             uint32_t *moved) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < words * 32u; v += stride) {
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, v < n && perm[v] != v);
+    if ((threadIdx.x & 31u) == 0) moved[v >> 5] = m;
+  }
+}
+
 // One warp per internal vertex: its list is the original list of perm[i],
 // every destination mapped through pinv.
 __global__ void relabel_kernel(const uint32_t *__restrict__ indptr,
@@ -129,6 +139,7 @@ void free_hub(bfs_graph *g) {
     cudaFree(h->inds);
     cudaFree(h->perm);
     cudaFree(h->pinv);
+    cudaFree(h->moved);
   }
   delete h;
   g->hub = nullptr;
@@ -156,7 +167,10 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
   if (!h) return fail(BFS_ERR_OOM, "host allocation failed");
   h->indptr = g->indptr;
   h->inds = g->inds;
-  if (n <= K || g->n_rows != n) {
+  // identity for small graphs, graphs whose rows are not all expanded and
+  // graphs of 2^31 vertices or more (level generation marks moved ids in
+  // bit 31 of its vertex lists)
+  if (n <= K || g->n_rows != n || n > 0x80000000u) {
     // identity: the prefix is the first min(K, all) original ids
     const uint32_t bits = (uint32_t)std::min<uint64_t>((uint64_t)K, (uint64_t)g->words * 32u);
     h->vertices = bits / 128u * 128u;
@@ -182,6 +196,7 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
   } while (0)
   HUB_CK(dev_malloc(&h->perm, sizeof(uint32_t) * (size_t)n));
   HUB_CK(dev_malloc(&h->pinv, sizeof(uint32_t) * (size_t)n));
+  HUB_CK(dev_malloc(&h->moved, sizeof(uint32_t) * (size_t)g->words));
   HUB_CK(dev_malloc(&h->indptr, sizeof(uint32_t) * ((size_t)n + 1)));
   HUB_CK(dev_malloc(&h->inds, sizeof(uint32_t) * (g->nnz ? g->nnz : 1)));
   HUB_CK(dev_malloc(&indeg, sizeof(uint32_t) * (size_t)n));
@@ -221,6 +236,7 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
   }
   pair_kernel<<<grid, 256, 0, s>>>(list_d, list_v, count, h->perm, h->pinv);
   finish_pinv_kernel<<<grid, 256, 0, s>>>(n, h->pinv, g->indptr, h->perm, deg);
+  moved_kernel<<<grid, 256, 0, s>>>(h->perm, n, g->words, h->moved);
   HUB_CK(cudaGetLastError());
   {
     size_t t = tmp_bytes;

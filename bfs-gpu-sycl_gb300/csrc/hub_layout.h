@@ -18,6 +18,7 @@ struct HubLayout {
   uint32_t *inds = nullptr;    // u32[nnz], relabelled destinations
   uint32_t *perm = nullptr;    // internal id -> original id
   uint32_t *pinv = nullptr;    // original id -> internal id
+  uint32_t *moved = nullptr;   // u32[words]: bit v set when perm[v] != v
   uint32_t vertices = 0;       // K: internal ids 0 .. K-1 are the hub prefix
   bool relabelled = false;
 };

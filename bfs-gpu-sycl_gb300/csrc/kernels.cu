@@ -371,6 +371,11 @@ __global__ void __launch_bounds__(B, (MinBlocks<B, U, STRIDED>::value))
 // blocks, so the global test-then-claim follows, and a claimed hub's bit is
 // then set in s_hub for the block's later probes (bits only ever go from 0
 // to 1, so any snapshot is a valid "already visited" set).
+// Chunks per lane and group of the chunk walk, whatever the ipt option: with
+// the next group's loads in flight that is 16 edge slots per lane, at the
+// 64 registers of a 1024-thread block (4 chunks per group spill).
+constexpr int kChunkGroup = 2;
+
 template <int U, bool PAR, bool HUB>
 __device__ __forceinline__ void explore_chunk_body(const BfsDevState *__restrict__ st,
                                                    uint32_t F, uint32_t gw,
@@ -393,6 +398,7 @@ __device__ __forceinline__ void explore_chunk_body(const BfsDevState *__restrict
   const uint32_t hi4 = (st->nnz + off) >> 2;
   uint32_t *vis = st->vis;
   const uint32_t *vis_c = vis;  // plain loads of the visited words
+  const uint32_t s_hub_addr = HUB ? (uint32_t)__cvta_generic_to_shared(s_hub) : 0u;
   int32_t *parent = PAR ? st->parent : nullptr;
   const uint32_t *perm = PAR ? st->perm : nullptr;
   const uint32_t lane = threadIdx.x & 31u;
@@ -483,35 +489,44 @@ __device__ __forceinline__ void explore_chunk_body(const BfsDevState *__restrict
         }
       }
     };
-    // Probes of the U chunks of a lane, in two phases: every slot's visited
-    // word is loaded (or, for an invalid slot or a hub the block already
-    // knows visited, replaced by its own bit) before any claim is issued --
-    // a claim is an asm statement that orders memory, so a load after it
-    // could not start before it.
+    // Probes of the U chunks of a lane, branch-free: for every slot a
+    // predicated shared load of the hub word (hub ids only), then a
+    // predicated global load of the visited word (valid slots the hub word
+    // did not show visited); a slot whose word shows its bit clear gets a
+    // bit in need[u].  Only then, behind one branch per chunk, the claims --
+    // a claim is an asm statement that orders memory, so no load may follow
+    // it within the group.
     auto probe = [&](const uint4 (&q)[U], const uint32_t (&m)[U], const uint32_t (&fr)[U]) {
-      uint32_t word[U][4];
+      uint32_t need[U];
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const uint32_t n4[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+        need[u] = 0u;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           const uint32_t n = n4[i];
           const uint32_t bit = 1u << (n & 31u);
-          bool known = !((m[u] >> i) & 1u);
-          if (HUB && !known && n < hub_lim) known = (s_hub[n >> 5] & bit) != 0u;
-          word[u][i] = known ? bit : vis_c[n >> 5];
+          uint32_t act = (m[u] >> i) & 1u;
+          if (HUB) {
+            uint32_t h = 0u;
+            ld_shared_if(h, s_hub_addr + ((n >> 5) << 2), act & (n < hub_lim ? 1u : 0u));
+            act &= (h & bit) ? 0u : 1u;
+          }
+          uint32_t word = bit;  // "visited" unless loaded
+          ld_global_if(word, vis_c + (n >> 5), act);
+          need[u] |= ((word & bit) ? 0u : 1u) << i;
         }
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
+        if (need[u] == 0u) continue;
         const uint32_t n4[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
 #pragma unroll
         for (int i = 0; i < 4; i++) {
+          if (!((need[u] >> i) & 1u)) continue;
           const uint32_t n = n4[i];
-          const uint32_t bit = 1u << (n & 31u);
-          if (word[u][i] & bit) continue;
           claim(vis, n, parent, fr[u], perm);
-          if (HUB && n < hub_lim) atomicOr(s_hub + (n >> 5), bit);
+          if (HUB && n < hub_lim) atomicOr(s_hub + (n >> 5), 1u << (n & 31u));
         }
       }
     };
@@ -536,16 +551,15 @@ __device__ __forceinline__ void explore_chunk_body(const BfsDevState *__restrict
 }
 
 // The GLB arms' own kernel (the engine runs GLB levels in explore_any; the
-// allocation-free entry point launches this one): 1024 threads per SM,
-// ipt / 2 chunks per lane and group.
+// allocation-free entry point launches this one): 1024 threads per SM.
 template <int B, int U, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B)
     explore_global_kernel(BfsDevState *__restrict__ st) {
   const uint32_t F = st->F;
   if (F == 0) return;
   note_arm<1 * 3 + BlockIndex<B>::value>(st);
-  explore_chunk_body<U / 2, PAR, false>(st, F, blockIdx.x * (B / 32) + (threadIdx.x >> 5),
-                                        gridDim.x * (B / 32), nullptr, 0u);
+  explore_chunk_body<kChunkGroup, PAR, false>(st, F, blockIdx.x * (B / 32) + (threadIdx.x >> 5),
+                                              gridDim.x * (B / 32), nullptr, 0u);
 }
 
 // ---- explore: any arm, chosen on the device ---------------------------------
@@ -555,10 +569,11 @@ __global__ void __launch_bounds__(B, 1024 / B)
 // scheduler stored in st->arm (init or the last block of the previous level
 // generation picked it), so the learned loop needs no switch node.
 //   GLB  the 16-byte chunk walk, chunks dealt per warp over the grid (the
-//        block size of the arm does not matter), ipt / 2 chunks per lane and
-//        group.  With a hub layout, levels of at least hub_min_edges edges
-//        first copy the hub prefix of the visited bitmap into the block's
-//        dynamic shared memory (s_hub) and probe through it.
+//        block size of the arm does not matter).  With a hub layout, levels
+//        of at least hub_min_edges edges, once at least half as many
+//        vertices as the prefix holds have been reached, first copy the hub
+//        prefix of the visited bitmap into the block's dynamic shared memory
+//        (s_hub) and probe through it.
 //   LLB / SLB  tiles of 128, 256 or 512 entries on 8, 4 or 2 slices of the
 //        block, each with its own shared arrays and named barrier.
 template <int U, bool PAR>
@@ -580,16 +595,18 @@ __global__ void __launch_bounds__(kAnyBlock, 1)
   const uint32_t t = threadIdx.x;
   if (form == BFS_LB_GLB) {
     const uint32_t hw = st->hub_words;  // a multiple of 4
-    const bool use = hw != 0 && st->EF >= st->hub_min_edges;  // uniform over the grid
+    // uniform over the grid; a level that reached fewer vertices than half
+    // the prefix would find few hubs visited and skips the copy
+    const bool use = hw != 0 && st->EF >= st->hub_min_edges && st->reached >= hw * 16u;
     if (use) {
       const uint4 *src = reinterpret_cast<const uint4 *>(st->vis);
       uint4 *dst = reinterpret_cast<uint4 *>(s_hub);
       for (uint32_t i = t; i < (hw >> 2); i += kAnyBlock) dst[i] = src[i];
       __syncthreads();
     }
-    explore_chunk_body<U / 2, PAR, true>(st, F, blockIdx.x * (kAnyBlock / 32) + (t >> 5),
-                                         gridDim.x * (kAnyBlock / 32), s_hub,
-                                         use ? hw * 32u : 0u);
+    explore_chunk_body<kChunkGroup, PAR, true>(st, F, blockIdx.x * (kAnyBlock / 32) + (t >> 5),
+                                               gridDim.x * (kAnyBlock / 32), s_hub,
+                                               use ? hw * 32u : 0u);
   } else if (bi == 2) {
     const uint32_t v = t >> 9, o = v * 513u;
     if (form == BFS_LB_SLB)
@@ -704,6 +721,10 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   uint32_t *__restrict__ qv = st->qv[nq];
   const uint32_t off = st->inds_off;
   const uint32_t *__restrict__ perm = st->perm;  // internal -> original (null: identity)
+  const uint32_t *__restrict__ moved = st->moved;  // bit v: perm[v] != v
+  // relabelled graphs have fewer than 2^31 vertices: bit 31 of a list entry
+  // is then free for the moved flag
+  const uint32_t id_mask = moved ? 0x7FFFFFFFu : 0xFFFFFFFFu;
   const bool want_vid = st->parent != nullptr;   // vertex ids are read for parents only
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -721,6 +742,9 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       const uint32_t vw = V[w0 + lane], pw = P[w0 + lane];
       uint32_t x = vw & ~pw;
       if (x) P[w0 + lane] = vw;
+      // under a relabelling, bit 31 of a list entry marks an id whose
+      // original id differs (the only ones that need a perm lookup)
+      const uint32_t mw = (moved && x) ? moved[w0 + lane] : 0u;
       const uint32_t c = __popc(x);
       const uint32_t incl = warp_incl_scan(c, lane);
       tot = __shfl_sync(kFull, incl, 31);
@@ -728,7 +752,8 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       const uint32_t vbase = (w0 + lane) * 32u;
       __syncwarp();  // the previous span's reads of the list are done
       while (x) {
-        list[pos++] = vbase + (uint32_t)(__ffs(x) - 1);
+        const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
+        list[pos++] = (vbase + bpos) | (((mw >> bpos) & 1u) << 31);
         x &= x - 1u;
       }
       __syncwarp();
@@ -745,8 +770,9 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
         const uint32_t t = t0 + 32u * r + lane;
         b[r] = e[r] = 0;
         if (t < tot) {
-          const uint32_t v = list[t];
-          level[perm ? perm[v] : v] = lvl_next;
+          const uint32_t ent = list[t];
+          const uint32_t v = ent & id_mask;
+          level[(ent & ~id_mask) ? perm[v] : v] = lvl_next;
           if (v < n_rows) {
             b[r] = indptr[v];
             e[r] = indptr[v + 1];
@@ -786,11 +812,13 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       uint32_t slot = (uint32_t)(wb >> 32), prefc = (uint32_t)wb;
       // pass 2: write the kept entries in the same order
       for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
-        uint32_t vv[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
+        uint32_t vv[kLgUnroll], mf[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
 #pragma unroll
         for (int r = 0; r < kLgUnroll; r++) {
           const uint32_t t = t0 + 32u * r + lane;
-          vv[r] = t < tot ? list[t] : kFull;
+          const uint32_t ent = t < tot ? list[t] : kFull;
+          vv[r] = t < tot ? (ent & id_mask) : kFull;
+          mf[r] = t < tot ? (ent & ~id_mask) : 0u;
           b[r] = e[r] = 0;
           if (vv[r] < n_rows) {  // kFull >= n_rows
             b[r] = indptr[vv[r]];
@@ -808,7 +836,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
             qb[sl] = b[r];
             qd[sl] = deg;
             qc[sl] = prefc + cincl - nch;
-            if (want_vid) qv[sl] = perm ? perm[vv[r]] : vv[r];
+            if (want_vid) qv[sl] = mf[r] ? perm[vv[r]] : vv[r];
           }
           slot += __popc(km);
           prefc += __shfl_sync(kFull, cincl, 31);

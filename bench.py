@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-arms", action="store_true", help="omit the per-arm table")
+    ap.add_argument("--skip-suites", action="store_true",
+                    help="omit the per-variant tables on RMAT-23, the 4096^2 grid and ER-2^22")
     return ap.parse_args()
 
 
@@ -177,6 +179,67 @@ def bfs_bytes(edges, reached, n):
     return 4.0 * edges + 16.0 * reached + 4.0 * n
 
 
+PLANS = [(lb, blk) for lb in ("llb", "glb", "slb") for blk in (128, 256, 512)]
+
+
+def suite_table(B, torch, graph, roots, weights, hbm_peak):
+    """Per-variant GTEPS, HBM GB/s (the bytes-moved formula of bfs_bytes over
+    each run's edges and reached vertices) and roofline fraction of the
+    single-root engine on one graph: every explore form x block size and the
+    learned schedule, the same roots for every plan, device time."""
+    n = graph.n_cols
+    lv = torch.empty(n, dtype=torch.int32, device="cuda")
+    plans = list(PLANS)
+    if weights is not None:
+        graph.sched_attach(weights)
+        plans.append(("learned", 256))
+    rows = {}
+    for lb, blk in plans:
+        o = B.options(lb, blk)
+        graph.run_device(int(roots[0]), lv.data_ptr(), opts=o)  # builds the loop graph
+        ms, edges, byts = 0.0, 0.0, 0.0
+        for r in roots:
+            st = graph.run_device(int(r), lv.data_ptr(), opts=o)
+            ms += st.device_ms
+            edges += st.edges_count
+            byts += bfs_bytes(st.edges_count, st.reached, n)
+        gbs = byts / (ms * 1e-3) / 1e9
+        rows["learned" if lb == "learned" else f"{lb}{blk}"] = {
+            "gteps": round(edges / (ms * 1e-3) / 1e9, 3), "ms_per_bfs": round(ms / len(roots), 4),
+            "hbm_gbs": round(gbs, 1), "roofline_frac": round(gbs / hbm_peak, 4)}
+    best = max((k for k in rows if k != "learned"), key=lambda k: rows[k]["gteps"])
+    out = {"variants": rows, "best_fixed": best}
+    if "learned" in rows:
+        out["learned_vs_best_fixed"] = round(rows["learned"]["gteps"] / rows[best]["gteps"], 3)
+        out["learned_vs_llb256"] = round(rows["learned"]["gteps"] / rows["llb256"]["gteps"], 3)
+    del lv
+    return out
+
+
+def run_suites(B, torch, weights, hbm_peak):
+    """BASELINE's configurations 2 and 3, measured per variant."""
+    res = {}
+    g = B.Graph.gen_rmat_device(23, 16, seed=2)
+    t = suite_table(B, torch, g, B.sample_roots(g.download(), 64, 2), weights, hbm_peak)
+    t["workload"] = ("RMAT-23/EF16 seed 2 (deduplicated, symmetrised), 64 seeded roots, "
+                     "graph level loop")
+    res["rmat23"] = t
+    g.free()
+    for key, make, roots_seed, label in (
+            ("grid4096", lambda: B.gen_grid(4096, 4096, 0.05, 3), 3,
+             "4096x4096 4-neighbour grid, 5% of edges deleted (seed 3), 32 seeded roots"),
+            ("er22", lambda: B.gen_er(1 << 22, 16.0, 4), 4,
+             "Erdos-Renyi, 2^22 vertices, average degree 16 (seed 4), 32 seeded roots")):
+        h = make()
+        g = B.Graph.upload(h, validate=False)
+        t = suite_table(B, torch, g, B.sample_roots(h, 32, roots_seed), weights, hbm_peak)
+        t["workload"] = label + ", graph level loop"
+        res[key] = t
+        g.free()
+        del h
+    return res
+
+
 def run_gb300(a):
     import numpy as np
     import torch
@@ -193,6 +256,10 @@ def run_gb300(a):
     host = dg.download()
     roots = B.sample_roots(host, a.warmup + a.steps + 8, a.seed + 1000 * rank)
     lv = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = time.perf_counter()
+    dg.hub_configure(-1)  # the default layout, built here rather than in the first run
+    hub_s = round(time.perf_counter() - t, 3)
+    hub = dg.hub_info()
     weights = None
     if os.path.exists(WEIGHTS):
         weights = np.fromfile(WEIGHTS, dtype="<f4")
@@ -413,6 +480,38 @@ def run_gb300(a):
                         "root each; one persistent CUDA-graph launch vs 256 single-graph BFS "
                         "(LLB/256, device time summed)"}
 
+    # learned scheduler regret on this held-out graph: every level of two
+    # roots timed with all 9 arms from the same state (bfs_sched_record), the
+    # model's choice from the level's features, against the per-level best
+    regret = None
+    if weights is not None and not a.skip_arms:
+        t_sel, t_best, t_llb, per_level = 0.0, 0.0, 0.0, []
+        for r in roots[a.warmup:a.warmup + 2]:
+            smp = dg.sched_record(int(r), reps=2)
+            feats = np.array([list(x.features) for x in smp], np.float32)
+            ms = np.array([list(x.arm_ms) for x in smp], np.float64)
+            chosen, _ = B.sched_predict(weights, feats)
+            for i in range(len(smp)):
+                best = ms[i].min()
+                t_sel += ms[i][chosen[i]]
+                t_best += best
+                t_llb += ms[i][1]
+                per_level.append(round(float(ms[i][chosen[i]] / best - 1.0), 4) if best > 0 else 0.0)
+        regret = {"explore_regret_frac": round(t_sel / t_best - 1.0, 4),
+                  "per_level_regret": per_level,
+                  "explore_speedup_vs_llb256": round(t_llb / t_sel, 3),
+                  "roots": 2, "levels": len(per_level),
+                  "method": "bfs_sched_record: every level timed with all 9 explore arms from the "
+                            "same state (best of 2); regret = time of the model's arm / best arm - 1"}
+    arms_best = None
+    if arms:
+        fixed = {k: v for k, v in arms.items() if k != "learned"}
+        arms_best = max(fixed, key=fixed.get)
+
+    suites = None
+    if not a.skip_suites:
+        suites = run_suites(B, torch, weights, hbm_peak)
+
     # CPU baseline: the oracle on one root, one thread (rank 0 only)
     cpu = None
     if rank == 0 and not a.skip_cpu:
@@ -468,10 +567,16 @@ def run_gb300(a):
         "validator_violations": int(bad),
         "fixed_llb256": {"value": round(llb_gteps, 4), "unit": UNIT},
         "learned_vs_fixed_llb256": round(value / llb_gteps, 3) if a.lb == "learned" else None,
+        "learned_vs_best_fixed": ({"best_fixed": arms_best,
+                                   "ratio": round(arms["learned"] / arms[arms_best], 4)}
+                                  if arms and "learned" in arms else None),
+        "scheduler_regret_rmat25": regret,
+        "hub_layout": {"vertices": hub[0], "relabelled": hub[1], "build_s": hub_s},
         "batched": batched,
         "batched_rmat25": batched25,
         "multigraph": multigraph,
         "arms_gteps": arms,
+        "suites": suites,
         "levels_first_root": lvl_rows,
     }
     if rank == 0:

@@ -579,7 +579,13 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
   s.level = levels_dev;
   s.parent = parents_dev;
   s.fixed_arm = arm;
-  if (g->hub) {
+  // The layout serves plans that run GLB levels (fixed GLB arms, the learned
+  // schedule, the per-level recorder).  Fixed LLB and SLB keep the original
+  // numbering: their tile-local balancing suffers when the hubs are
+  // consecutive ids, i.e. consecutive queue entries.
+  const bool use_hub = g->hub != nullptr &&
+                       (o.lb == BFS_LB_GLB || o.lb == BFS_LB_LEARNED || timer != nullptr);
+  if (use_hub) {
     s.indptr = g->hub->indptr;
     s.inds = g->hub->inds;
     s.inds_off = (uint32_t)((reinterpret_cast<uintptr_t>(g->hub->inds) & 15u) >> 2);

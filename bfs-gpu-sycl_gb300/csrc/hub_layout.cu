@@ -24,6 +24,11 @@
 // Level and parent arrays are still written in original ids (the level
 // generation kernel writes level[perm[v]]), so callers see no difference.
 //
+// A graph whose K highest in-degree vertices take less than a quarter of all
+// edge endpoints (grids, uniform random graphs) gets no layout at all: the
+// prefix would catch few probes, and the copy would cost memory and the
+// shared-memory copy time for nothing.
+//
 // Graphs with n_cols <= K need no relabelling: the whole bitmap fits in
 // shared memory and the layout is the identity (no copy).  Graphs with
 // n_rows < n_cols keep the identity too (a relabelling could move a vertex
@@ -58,6 +63,16 @@ __global__ void init_perm_kernel(uint32_t n, uint32_t *iota, uint32_t *perm, uin
     perm[v] = v;
     pinv[v] = kNone;
   }
+}
+
+// Sum of the K largest in-degrees (the edge endpoints the prefix covers).
+__global__ void top_sum_kernel(const uint32_t *__restrict__ sorted_deg, uint32_t K,
+                               unsigned long long *sum) {
+  unsigned long long t = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
+    t += sorted_deg[i];
+  for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, d);
+  if ((threadIdx.x & 31u) == 0 && t) atomicAdd(sum, t);
 }
 
 // internal i < K takes the i-th vertex by in-degree
@@ -184,6 +199,8 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
   cudaStream_t s = g->stream;
   uint32_t *indeg = nullptr, *iota = nullptr, *sorted_deg = nullptr, *by_degree = nullptr;
   uint32_t *list_d = nullptr, *list_v = nullptr, *count = nullptr, *deg = nullptr;
+  unsigned long long *cover = nullptr, h_cover = 0;
+  bool flat = false;
   uint8_t *flags = nullptr;
   void *tmp = nullptr;
   size_t tmp_bytes = 0, t_sort = 0, t_sel = 0, t_scan = 0;
@@ -206,6 +223,7 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
   HUB_CK(dev_malloc(&list_d, sizeof(uint32_t) * (size_t)K));
   HUB_CK(dev_malloc(&list_v, sizeof(uint32_t) * (size_t)K));
   HUB_CK(dev_malloc(&count, sizeof(uint32_t) * 2));
+  HUB_CK(dev_malloc(&cover, sizeof(unsigned long long)));
   HUB_CK(dev_malloc(&deg, sizeof(uint32_t) * ((size_t)n + 1)));
   HUB_CK(dev_malloc(&flags, 2 * (size_t)n));
   HUB_CK(cub::DeviceRadixSort::SortPairsDescending(nullptr, t_sort, indeg, sorted_deg, iota,
@@ -224,6 +242,14 @@ bfs_status build_hub(bfs_graph *g, uint32_t K) {
     size_t t = tmp_bytes;
     HUB_CK(cub::DeviceRadixSort::SortPairsDescending(tmp, t, indeg, sorted_deg, iota, by_degree,
                                                      (int64_t)n, 0, 32, s));
+  }
+  HUB_CK(cudaMemsetAsync(cover, 0, sizeof(unsigned long long), s));
+  top_sum_kernel<<<grid, 256, 0, s>>>(sorted_deg, K, cover);
+  HUB_CK(cudaMemcpyAsync(&h_cover, cover, sizeof(h_cover), cudaMemcpyDeviceToHost, s));
+  HUB_CK(cudaStreamSynchronize(s));
+  if (h_cover * 4ull < g->nnz) {
+    flat = true;  // no hubs to speak of: no layout
+    goto done;
   }
   place_hubs_kernel<<<grid, 256, 0, s>>>(by_degree, K, h->perm, h->pinv);
   flags_kernel<<<grid, 256, 0, s>>>(h->pinv, K, n, flags, flags + n);
@@ -263,13 +289,15 @@ done:
   cudaFree(list_d);
   cudaFree(list_v);
   cudaFree(count);
+  cudaFree(cover);
   cudaFree(deg);
   cudaFree(flags);
   cudaFree(tmp);
-  if (e != cudaSuccess) {
+  if (e != cudaSuccess || flat) {
     cudaGetLastError();
     g->hub = h;  // frees the layout's own arrays, never the graph's
     free_hub(g);
+    if (flat) return BFS_OK;
     if (e == cudaErrorMemoryAllocation) return BFS_OK;  // no layout: plain kernels
     return fail(BFS_ERR_CUDA, std::string("hub layout: ") + cudaGetErrorString(e));
   }

@@ -137,8 +137,11 @@ bfs_status bfs_graph_device_csc(const bfs_graph *g, const uint32_t **d_indptr,
  * shared memory.  For that the handle keeps a relabelled copy of the graph
  * whose internal ids 0 .. K-1 are its K highest in-degree vertices (graphs
  * of at most K vertices, and graphs with n_rows < n_cols, keep their own ids
- * and no copy).  Levels, parents and every other entry point still use the
- * caller's ids; results are identical with or without the layout.  The copy
+ * and no copy).  The layout serves runs whose plan runs GLB levels (fixed
+ * GLB arms and the learned schedule); fixed LLB and SLB runs keep the
+ * original numbering, since their tile-local balancing suffers when the hubs
+ * are consecutive ids.  Levels, parents and every other entry point still
+ * use the caller's ids; results are identical with or without the layout.  The copy
  * costs nnz + 3 n_cols + 1 uint32 of device memory; if it cannot be
  * allocated the handle runs without it.
  * vertices: -1 = automatic (the default: K = 2^18, capped by the device's

@@ -49,7 +49,7 @@ SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz) {
 __global__ void sched_kernel(BfsDevState *st, const float *__restrict__ w, float min_conf,
                              SchedGraphConst gc) {
   if (threadIdx.x >= 32) return;
-  sched_pick_warp(st, w, min_conf, gc);
+  sched_pick_warp<false>(st, w, min_conf, gc);
   if (threadIdx.x == 0) st->launches += 1;
 }
 
@@ -72,7 +72,7 @@ __global__ void predict_kernel(const float *__restrict__ w, const float *__restr
     for (int i = 0; i < kSchedIn; i++) x[i] = X[(size_t)s * kSchedIn + i];
     float h1, h2, pbest;
     int best;
-    const float z = mlp_forward(w, x, lane, &h1, &h2);
+    const float z = mlp_forward<false>(w, x, lane, &h1, &h2);
     softmax9(z, lane, &best, &pbest);
     if (lane == 0) {
       if (arms) arms[s] = best;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) train_grad_kernel(const float *__restrict
     for (int i = 0; i < kSchedIn; i++) x[i] = X[(size_t)s * kSchedIn + i];
     float h1, h2, pbest;
     int best;
-    const float z = mlp_forward(w, x, lane, &h1, &h2);
+    const float z = mlp_forward<false>(w, x, lane, &h1, &h2);
     const float p = softmax9(z, lane, &best, &pbest);
     const float c = out_lane ? Cst[(size_t)s * kSchedArms + lane] : 0.f;
     float ec = p * c;

@@ -22,7 +22,13 @@ __device__ __forceinline__ void level_features(const BfsDevState *st, SchedGraph
 }
 
 // Forward pass of one sample by one warp.  Returns this lane's output logit
-// (meaningful on lanes < 9) and the lane's hidden activations.
+// (meaningful on lanes < 9) and the lane's hidden activations.  TRANSPOSED:
+// W2 and W3 are stored column-major (W2[k][j] at kW2 + 32 k + j, W3[k][a] at
+// kW3 + 9 k + a), the shared-memory copy the level loop stages, so that the
+// 32 lanes read 32 different banks; otherwise the row-major layout of the
+// parameter vector.  The dot products keep four partial sums (k mod 4), in
+// the same order for both layouts, so every caller gets identical logits.
+template <bool TRANSPOSED>
 __device__ __forceinline__ float mlp_forward(const float *__restrict__ w,
                                              const float x[kSchedIn], uint32_t lane,
                                              float *h1_out, float *h2_out) {
@@ -30,21 +36,38 @@ __device__ __forceinline__ float mlp_forward(const float *__restrict__ w,
 #pragma unroll
   for (int i = 0; i < kSchedIn; i++) a = fmaf(w[kW1 + lane * kSchedIn + i], x[i], a);
   const float h1 = fmaxf(a, 0.f);
-  float b = w[kB2 + lane];
-#pragma unroll 8
-  for (int k = 0; k < kSchedHidden; k++)
-    b = fmaf(w[kW2 + lane * kSchedHidden + k], __shfl_sync(kFullMask, h1, k), b);
-  const float h2 = fmaxf(b, 0.f);
+  float b[4] = {w[kB2 + lane], 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < kSchedHidden; k++) {
+    const float wk = TRANSPOSED ? w[kW2 + k * kSchedHidden + lane] : w[kW2 + lane * kSchedHidden + k];
+    b[k & 3] = fmaf(wk, __shfl_sync(kFullMask, h1, k), b[k & 3]);
+  }
+  const float h2 = fmaxf((b[0] + b[1]) + (b[2] + b[3]), 0.f);
   const bool out_lane = lane < (uint32_t)kSchedArms;
-  float c = out_lane ? w[kB3 + lane] : 0.f;
-#pragma unroll 8
+  const uint32_t ol = out_lane ? lane : 0u;
+  float c[4] = {out_lane ? w[kB3 + lane] : 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
   for (int k = 0; k < kSchedHidden; k++) {
     const float hk = __shfl_sync(kFullMask, h2, k);
-    if (out_lane) c = fmaf(w[kW3 + lane * kSchedHidden + k], hk, c);
+    const float wk = TRANSPOSED ? w[kW3 + k * kSchedArms + ol] : w[kW3 + ol * kSchedHidden + k];
+    if (out_lane) c[k & 3] = fmaf(wk, hk, c[k & 3]);
   }
   *h1_out = h1;
   *h2_out = h2;
-  return c;
+  return (c[0] + c[1]) + (c[2] + c[3]);
+}
+
+// Index of parameter i in the transposed (shared-memory) layout.
+__host__ __device__ __forceinline__ int sched_transposed_index(int i) {
+  if (i >= kW2 && i < kB2) {
+    const int j = (i - kW2) / kSchedHidden, k = (i - kW2) % kSchedHidden;
+    return kW2 + k * kSchedHidden + j;
+  }
+  if (i >= kW3 && i < kB3) {
+    const int a = (i - kW3) / kSchedHidden, k = (i - kW3) % kSchedHidden;
+    return kW3 + k * kSchedArms + a;
+  }
+  return i;
 }
 
 // Softmax over lanes 0..8: returns p on output lanes, 0 elsewhere; *best and
@@ -74,6 +97,7 @@ __device__ __forceinline__ float softmax9(float z, uint32_t lane, int *best, flo
 // One warp: the arm for the state's current level (kFallbackArm without a
 // model, on an empty frontier or below min_conf).  Lane 0 stores it in
 // st->arm and the level record.
+template <bool TRANSPOSED>
 __device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__restrict__ w,
                                                float min_conf, SchedGraphConst gc) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -83,13 +107,15 @@ __device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__r
     level_features(st, gc, x);
     float h1, h2, pbest;
     int best;
-    const float z = mlp_forward(w, x, lane, &h1, &h2);
+    const float z = mlp_forward<TRANSPOSED>(w, x, lane, &h1, &h2);
     softmax9(z, lane, &best, &pbest);
     arm = (pbest >= min_conf) ? best : kFallbackArm;
   }
   if (lane == 0) {
     st->arm = arm;
     if (st->lvl < st->rec_cap) st->rec_arm[st->lvl] = arm;
+    // the CUDA-graph loop's switch node launches this arm's explore kernel
+    if (st->sw_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)st->sw_handle, (unsigned)arm);
   }
   return arm;
 }

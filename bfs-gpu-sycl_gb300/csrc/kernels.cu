@@ -136,11 +136,13 @@ __device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w) {
   SchedGraphConst gc;
   gc.diam = st->sched_diam;
   gc.avg_deg_x = st->sched_avg_deg_x;
-  sched_pick_warp(st, w, st->sched_min_conf, gc);
+  sched_pick_warp<true>(st, w, st->sched_min_conf, gc);
 }
 
 // Copies the model to shared memory with all threads of the block: one
-// round of parallel loads instead of the MLP's dependent ones.  The loads
+// round of parallel loads instead of the MLP's dependent ones; W2 and W3 are
+// stored transposed there (sched_transposed_index), so that the warp reads
+// them without bank conflicts.  The loads
 // mark the model evict-last in L2, so that it stays there while each level's
 // edge stream (evict-first) passes through.
 __device__ __forceinline__ void stage_weights(float *dst, const float *__restrict__ w) {
@@ -149,7 +151,7 @@ __device__ __forceinline__ void stage_weights(float *dst, const float *__restric
   for (uint32_t i = threadIdx.x; i < (uint32_t)kSchedParams; i += blockDim.x) {
     float x;
     asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(w + i), "l"(pol));
-    dst[i] = x;
+    dst[sched_transposed_index((int)i)] = x;
   }
 }
 

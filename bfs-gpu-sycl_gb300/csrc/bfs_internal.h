@@ -138,7 +138,6 @@ struct BfsDevState {
   // generation (CUDA-graph loop): it stores the next level's explore arm in
   // `arm`, which explore_any then runs
   const float *sched_w;      // model weights; null: the scheduler is not fused
-  unsigned long long sw_handle;  // switch node of the loop (0: none): set to the arm
   float sched_min_conf;      // below this top probability: the fallback arm
   float sched_diam;          // graph-level feature constants
   float sched_avg_deg_x;

@@ -49,14 +49,14 @@ SchedGraphConst sched_graph_const(uint32_t n_cols, uint64_t nnz) {
 __global__ void sched_kernel(BfsDevState *st, const float *__restrict__ w, float min_conf,
                              SchedGraphConst gc) {
   if (threadIdx.x >= 32) return;
-  sched_pick_warp<false>(st, w, min_conf, gc);
+  sched_pick_warp<false>(st, level_counters(st), w, min_conf, gc);
   if (threadIdx.x == 0) st->launches += 1;
 }
 
 __global__ void features_kernel(const BfsDevState *st, SchedGraphConst gc, float *out) {
   if (threadIdx.x == 0) {
     float x[kSchedIn];
-    level_features(st, gc, x);
+    level_features(level_counters(st), st->n_cols, gc, x);
     for (int i = 0; i < kSchedIn; i++) out[i] = x[i];
   }
 }

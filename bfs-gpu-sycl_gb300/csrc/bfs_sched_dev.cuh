@@ -12,12 +12,21 @@ namespace bfsgb {
 
 constexpr uint32_t kFullMask = 0xFFFFFFFFu;
 
-__device__ __forceinline__ void level_features(const BfsDevState *st, SchedGraphConst gc,
-                                               float x[kSchedIn]) {
-  x[0] = log2f(1.f + (float)st->F) / 32.f;
-  x[1] = log2f(1.f + (float)st->EF) / 32.f;
-  x[2] = 1.f - (float)st->reached / (float)st->n_cols;
-  x[3] = fminf((float)st->lvl / gc.diam, 8.f) / 8.f;
+// The level counters the features are made of.
+struct LevelCounters {
+  uint32_t F, EF, reached, lvl;
+};
+
+__device__ __forceinline__ LevelCounters level_counters(const BfsDevState *st) {
+  return LevelCounters{st->F, st->EF, st->reached, st->lvl};
+}
+
+__device__ __forceinline__ void level_features(const LevelCounters &c, uint32_t n_cols,
+                                               SchedGraphConst gc, float x[kSchedIn]) {
+  x[0] = log2f(1.f + (float)c.F) / 32.f;
+  x[1] = log2f(1.f + (float)c.EF) / 32.f;
+  x[2] = 1.f - (float)c.reached / (float)n_cols;
+  x[3] = fminf((float)c.lvl / gc.diam, 8.f) / 8.f;
   x[4] = gc.avg_deg_x;
 }
 
@@ -94,17 +103,18 @@ __device__ __forceinline__ float softmax9(float z, uint32_t lane, int *best, flo
   return e / s;
 }
 
-// One warp: the arm for the state's current level (kFallbackArm without a
-// model, on an empty frontier or below min_conf).  Lane 0 stores it in
+// One warp: the arm for the level whose counters are c (kFallbackArm without
+// a model, on an empty frontier or below min_conf).  Lane 0 stores it in
 // st->arm and the level record.
 template <bool TRANSPOSED>
-__device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__restrict__ w,
-                                               float min_conf, SchedGraphConst gc) {
+__device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const LevelCounters &c,
+                                               const float *__restrict__ w, float min_conf,
+                                               SchedGraphConst gc) {
   const uint32_t lane = threadIdx.x & 31u;
   int arm = kFallbackArm;
-  if (w != nullptr && st->F > 0) {
+  if (w != nullptr && c.F > 0) {
     float x[kSchedIn];
-    level_features(st, gc, x);
+    level_features(c, st->n_cols, gc, x);
     float h1, h2, pbest;
     int best;
     const float z = mlp_forward<TRANSPOSED>(w, x, lane, &h1, &h2);
@@ -113,9 +123,7 @@ __device__ __forceinline__ int sched_pick_warp(BfsDevState *st, const float *__r
   }
   if (lane == 0) {
     st->arm = arm;
-    if (st->lvl < st->rec_cap) st->rec_arm[st->lvl] = arm;
-    // the CUDA-graph loop's switch node launches this arm's explore kernel
-    if (st->sw_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)st->sw_handle, (unsigned)arm);
+    if (c.lvl < st->rec_cap) st->rec_arm[c.lvl] = arm;
   }
   return arm;
 }

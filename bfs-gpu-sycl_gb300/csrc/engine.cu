@@ -372,11 +372,11 @@ static cudaError_t add_kernel(cudaGraph_t graph, cudaGraphNode_t *node,
 //   fill(levels/parents, bitmaps) -> init(root) -> while(F > 0) {
 //     explore -> levelgen (last block sets the while condition) }
 // With a fixed arm the explore node is that arm's kernel (explore_any for the
-// GLB arms).  With arm < 0 (learned schedule) it is a switch node with one
-// body per arm -- that arm's own kernel, the one the per-level recorder
-// times -- whose value the scheduler sets: it runs inside init (level 0) and
-// inside the last block of level generation (the next level), so the loop
-// has no node of its own for it.
+// GLB arms).  With arm < 0 (learned schedule) it is explore_any, which runs
+// the arm in st->arm: the scheduler runs inside init (level 0) and inside the
+// last block of level generation (the next level), so the loop has no node
+// of its own for it.  (A switch node selecting each arm's own kernel was
+// measured: about 4.5 us more per level than explore_any's uniform branch.)
 static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt,
                                    GraphEntry *ge) {
   cudaGraph_t graph = nullptr;
@@ -405,41 +405,16 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   cudaGraph_t body = wp.conditional.phGraph_out[0];
 
   void *ex_args[] = {&st};
-  int arm_args[kNumArms];
-  void *any_args[kNumArms][2];
-  for (int a = 0; a < kNumArms; a++) {
-    arm_args[a] = a;
-    any_args[a][0] = &st;
-    any_args[a][1] = &arm_args[a];
-  }
-  // explore node of one arm in graph gr
-  auto add_arm = [&](cudaGraph_t gr, int a, cudaGraphNode_t *node) -> cudaError_t {
-    if (arm_lb(a) == BFS_LB_GLB)
-      return add_kernel(gr, node, nullptr, 0, explore_any_kernel_fn(ipt, g->run_parents),
-                        any_blocks(g, ipt), kAnyBlock, any_args[a], hub_smem(g));
-    return add_kernel(gr, node, nullptr, 0, explore_kernel_fn(a, ipt, g->run_parents),
-                      persistent_blocks(g, a, sm_factor, ipt), arm_block(a), ex_args);
-  };
-  if (arm >= 0) {
-    CK(add_arm(body, arm, &n_explore));
-    set_window(g, n_explore);
+  int arm_arg = arm;  // < 0: the scheduler's arm in st->arm
+  void *any_args[] = {&st, &arm_arg};
+  if (arm >= 0 && arm_lb(arm) != BFS_LB_GLB) {
+    CK(add_kernel(body, &n_explore, nullptr, 0, explore_kernel_fn(arm, ipt, g->run_parents),
+                  persistent_blocks(g, arm, sm_factor, ipt), arm_block(arm), ex_args));
   } else {
-    cudaGraphConditionalHandle sw;
-    CK(cudaGraphConditionalHandleCreate(&sw, graph, (unsigned)kFallbackArm, 0));
-    ge->sw = (unsigned long long)sw;
-    alignas(cudaGraphNodeParams) unsigned char sbuf[sizeof(cudaGraphNodeParams)] = {};
-    cudaGraphNodeParams &sp = *reinterpret_cast<cudaGraphNodeParams *>(sbuf);
-    sp.type = cudaGraphNodeTypeConditional;
-    sp.conditional.handle = sw;
-    sp.conditional.type = cudaGraphCondTypeSwitch;
-    sp.conditional.size = kNumArms;
-    CK(cudaGraphAddNode(&n_explore, body, nullptr, nullptr, 0, &sp));
-    for (int a = 0; a < kNumArms; a++) {
-      cudaGraphNode_t n_arm;
-      CK(add_arm(sp.conditional.phGraph_out[a], a, &n_arm));
-      set_window(g, n_arm);
-    }
+    CK(add_kernel(body, &n_explore, nullptr, 0, explore_any_kernel_fn(ipt, g->run_parents),
+                  any_blocks(g, ipt), kAnyBlock, any_args, hub_smem(g)));
   }
+  set_window(g, n_explore);
   void *lg_args[] = {&st, &cond_arg, &one};
   CK(add_kernel(body, &n_lg, &n_explore, 1, levelgen_kernel_fn(), g->lg_grid, kLevelgenBlock,
                 lg_args));
@@ -631,7 +606,6 @@ bfs_status run_device_impl(bfs_graph *g, uint32_t root, const bfs_options *opts_
     if (rc != BFS_OK) return rc;
     if (arm < 0) {  // scheduler fused into init and level generation
       const SchedGraphConst gc = sched_graph_const(g->n_cols, g->nnz);
-      s.sw_handle = ge->sw;
       s.sched_w = g->sched->d_w;
       s.sched_min_conf = g->sched->min_conf;
       s.sched_diam = gc.diam;

@@ -13,7 +13,6 @@ namespace bfsgb {
 struct GraphEntry {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  unsigned long long sw = 0;  // switch handle of the learned loop (0: none)
 };
 
 struct SchedModel;

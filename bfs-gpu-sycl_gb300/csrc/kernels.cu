@@ -128,15 +128,16 @@ struct BlockIndex {
   static constexpr int value = B == 128 ? 0 : B == 256 ? 1 : 2;
 };
 
-// One warp: the learned scheduler's arm for the state's current level, from
+// One warp: the learned scheduler's arm for the level with counters c, from
 // the weights w (staged in shared memory by the caller) and the graph
 // constants held in the state, stored in st->arm for explore_any.  Kept out
 // of line so that the callers' register allocation is not affected.
-__device__ __noinline__ void fused_sched_pick(BfsDevState *st, const float *w) {
+__device__ __noinline__ void fused_sched_pick(BfsDevState *st, const LevelCounters &c,
+                                               const float *w) {
   SchedGraphConst gc;
   gc.diam = st->sched_diam;
   gc.avg_deg_x = st->sched_avg_deg_x;
-  sched_pick_warp<true>(st, w, st->sched_min_conf, gc);
+  sched_pick_warp<true>(st, c, w, st->sched_min_conf, gc);
 }
 
 // Copies the model to shared memory with all threads of the block: one
@@ -214,7 +215,7 @@ __global__ void init_kernel(BfsDevState *st, unsigned long long cond, int use_co
   if (w != nullptr) stage_weights(s_w, w);
   if (threadIdx.x == 0) init_state(st, cond, use_cond);
   __syncwarp();
-  if (w != nullptr) fused_sched_pick(st, s_w);
+  if (w != nullptr) fused_sched_pick(st, level_counters(st), s_w);
 }
 
 // ---- explore: LLB / SLB -----------------------------------------------------
@@ -643,7 +644,9 @@ __global__ void __launch_bounds__(kAnyBlock, 1)
 }
 
 // ---- level generation -----------------------------------------------------
-__device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_cond) {
+// Returns the new level's counters (for the fused scheduler, without a
+// round trip through global memory).
+__device__ LevelCounters finish_level(BfsDevState *st, unsigned long long cond, int use_cond) {
   const unsigned long long packed = *(volatile unsigned long long *)&st->next_packed;
   const uint32_t f_new = (uint32_t)(packed >> 32);
   const uint32_t ec_new = (uint32_t)packed;
@@ -675,6 +678,7 @@ __device__ void finish_level(BfsDevState *st, unsigned long long cond, int use_c
     st->F = 0;
   }
   if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, st->F > 0);
+  return LevelCounters{st->F, ef_new, reached, lvl};
 }
 
 // Level generation.  Blocks claim spans of NW * 32 bitmap words from a
@@ -708,6 +712,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   __shared__ uint32_t s_sb[2];
   __shared__ uint32_t s_reached[NW];
   __shared__ int s_last;
+  __shared__ LevelCounters s_ctr;
 
   const uint32_t words = st->words;
   uint32_t *__restrict__ V = st->vis;
@@ -871,10 +876,10 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     if (w != nullptr) stage_weights(s_w, w);
     if (threadIdx.x == 0) {
       __threadfence();
-      finish_level(st, cond, use_cond);
+      s_ctr = finish_level(st, cond, use_cond);
     }
     __syncthreads();
-    if (w != nullptr && warp == 0) fused_sched_pick(st, s_w);
+    if (w != nullptr && warp == 0) fused_sched_pick(st, s_ctr, s_w);
   }
 }
 

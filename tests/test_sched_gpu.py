@@ -140,7 +140,7 @@ def test_device_choice_equals_batch_prediction(B):
 
 def test_graph_loop_runs_every_arm_exactly(B, O):
     """A model whose output bias forces one arm runs that arm on every level
-    of the CUDA-graph loop (the switch node's body of that arm), with and
+    of the CUDA-graph loop (the one kernel that serves any arm), with and
     without parents; levels, edge counts and parents are exact."""
     torch_cuda()
     graphs = [B.gen_rmat(15, 16, seed=21), B.gen_grid(96, 64, 0.05, 22)]

@@ -146,10 +146,12 @@ __device__ __noinline__ void fused_sched_pick(BfsDevState *st, const LevelCounte
 // them without bank conflicts.  The loads
 // mark the model evict-last in L2, so that it stays there while each level's
 // edge stream (evict-first) passes through.
-__device__ __forceinline__ void stage_weights(float *dst, const float *__restrict__ w) {
+// Threads first .. blockDim.x - 1 take part.
+__device__ __forceinline__ void stage_weights(float *dst, const float *__restrict__ w,
+                                              uint32_t first = 0) {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  for (uint32_t i = threadIdx.x; i < (uint32_t)kSchedParams; i += blockDim.x) {
+  for (uint32_t i = threadIdx.x - first; i < (uint32_t)kSchedParams; i += blockDim.x - first) {
     float x;
     asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(w + i), "l"(pol));
     dst[sched_transposed_index((int)i)] = x;
@@ -871,12 +873,15 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     // explore_any launch of the next loop iteration.  The block copies the
     // model into the (now unused) vertex-list buffer while thread 0 closes
     // the level.
+    // (thread 0 stays out of the copy: its fence before closing the level
+    // would otherwise wait for its share of the model's loads)
     const float *w = st->sched_w;
     float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
-    if (w != nullptr) stage_weights(s_w, w);
     if (threadIdx.x == 0) {
       __threadfence();
       s_ctr = finish_level(st, cond, use_cond);
+    } else if (w != nullptr) {
+      stage_weights(s_w, w, 1u);
     }
     __syncthreads();
     if (w != nullptr && warp == 0) fused_sched_pick(st, s_ctr, s_w);

@@ -523,6 +523,7 @@ bfs_status ensure_hub(bfs_graph *g) {
   if (g->hub_tried && g->hub_built_for == want) return BFS_OK;
   g->hub_tried = true;
   g->hub_built_for = want;
+  g->hub_gen++;  // workspaces that copied the layout's pointers rebuild
   bfs_status rc = build_hub(g, want);
   // cached loop graphs were built for the previous layout's launch shapes
   for (auto &kv : g->graphs) {

@@ -100,5 +100,6 @@ struct bfs_graph {
   uint32_t hub_max = 0;        // largest prefix the device's shared memory holds
   uint32_t hub_min_edges = 0;  // level size from which explore loads it (0: automatic)
   uint32_t hub_built_for = 0;  // the request the current layout was built for
+  uint32_t hub_gen = 0;        // bumped whenever the layout is rebuilt or freed
   bool hub_tried = false;
 };

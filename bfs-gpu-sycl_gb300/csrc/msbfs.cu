@@ -31,6 +31,16 @@
 //             the search goes past the history it runs at that point and the
 //             deeper levels are stored into the rows directly.
 //   loop      a CUDA graph with a conditional WHILE node, as for one root.
+//
+// With the graph handle's hub layout (hub_layout.cu) the batch runs on the
+// relabelled graph, whose internal ids 0 .. K-1 are the K highest in-degree
+// vertices: level generation also writes a bitmap of the hub ids every root
+// of the pass has reached (hubfull), explore copies it into shared memory on
+// large levels and skips the 8-byte mask probe of those targets -- on
+// power-law graphs most edges of the later levels point at them, and the
+// mask array is larger than L2, so each probe skipped is a DRAM sector
+// saved.  Rows are written in original ids (expand reads the internal state
+// through pinv).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,6 +52,7 @@
 #include "dev_alloc.h"
 #include "device_util.cuh"
 #include "engine.h"
+#include "hub_layout.h"
 #include "kernels.h"
 
 namespace bfsgb {
@@ -64,6 +75,11 @@ struct MsState {
   uint32_t *qp[2];
   unsigned long long *qm[2];
   int32_t *level;  // n_lanes rows of n_cols
+  // hub layout (null: identity ids, no filter)
+  const uint32_t *perm, *pinv, *moved;
+  uint32_t *hubfull;       // bit v (v < 32 hub_words): every root has reached v
+  uint32_t hub_words;      // words of hubfull (0: no filter)
+  uint32_t hub_min_edges;  // frontier edges from which explore loads it
   uint32_t n_lanes;
   uint32_t roots[kLanes];
   unsigned long long next_packed;
@@ -77,8 +93,9 @@ struct MsState {
 // (roots shared by several lanes become one entry with several mask bits).
 __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_cond) {
   const uint32_t j = threadIdx.x;
+  const uint32_t *pinv = st->pinv;  // roots are original ids
   if (j < st->n_lanes) {
-    const uint32_t r = st->roots[j];
+    const uint32_t r = pinv ? pinv[st->roots[j]] : st->roots[j];
     atomicOr(&st->vis[r], 1ull << j);
     atomicOr(&st->prev[r], 1ull << j);
     atomicOr(&st->hist[r], 1ull << j);  // level 0
@@ -88,7 +105,7 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
   if (j == 0) {
     uint32_t F = 0, EF = 0;
     for (uint32_t l = 0; l < st->n_lanes; l++) {
-      const uint32_t r = st->roots[l];
+      const uint32_t r = pinv ? pinv[st->roots[l]] : st->roots[l];
       if (r >= st->n_rows) continue;
       const uint32_t b = st->indptr[r], e = st->indptr[r + 1];
       if (e == b) continue;
@@ -127,12 +144,22 @@ __global__ void ms_init_kernel(MsState *st, unsigned long long cond, int use_con
 // which costs only a redundant reduction.
 __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
     ms_explore_kernel(MsState *__restrict__ st) {
+  extern __shared__ __align__(16) uint32_t s_full[];  // hubfull, hub_words words
   constexpr int NW = kMsBlock / 32;
   constexpr int U = kMsU;
   constexpr uint32_t kRound = 32u * U;
   const uint32_t F = st->F;
   if (F == 0) return;
   const uint32_t EF = st->EF;
+  const uint32_t hw = st->hub_words;  // a multiple of 4
+  const bool use_hub = hw != 0 && EF >= st->hub_min_edges;  // uniform over the grid
+  if (use_hub) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(st->hubfull);
+    uint4 *dst = reinterpret_cast<uint4 *>(s_full);
+    for (uint32_t i = threadIdx.x; i < (hw >> 2); i += kMsBlock) dst[i] = src[i];
+    __syncthreads();
+  }
+  const uint32_t hub_lim = use_hub ? hw * 32u : 0u;
   const uint32_t cq = st->cur;
   const uint32_t *__restrict__ qb = st->qb[cq];
   const uint32_t *__restrict__ qp = st->qp[cq];
@@ -190,6 +217,8 @@ __global__ void __launch_bounds__(kMsBlock, 1536 / kMsBlock)
 #pragma unroll
       for (int u = 0; u < U; u++) {
         if (nb[u] == kFull) continue;
+        // a hub every root had reached by the previous level needs no probe
+        if (nb[u] < hub_lim && ((s_full[nb[u] >> 5] >> (nb[u] & 31u)) & 1u)) continue;
         // roots not yet in v's live mask (it holds the roots of earlier levels
         // and those other edges gave v in this level): only new roots cost a
         // reduction.  A target every root has reached needs no root mask.
@@ -252,6 +281,12 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
   unsigned long long *__restrict__ qm = st->qm[nq];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
+  const unsigned long long all_roots =
+      st->n_lanes >= 64u ? ~0ull : (1ull << st->n_lanes) - 1ull;
+  uint32_t *__restrict__ hubfull = st->hubfull;
+  const uint32_t hub_words = st->hub_words;
+  const uint32_t *__restrict__ perm = st->perm;
+  const uint32_t *__restrict__ moved = st->moved;
   if (threadIdx.x == 0) s_any = 0;
   __syncthreads();
   bool any = false;
@@ -260,8 +295,10 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
     const uint32_t v = (uint32_t)(sb + threadIdx.x);
     unsigned long long nw = 0;
     uint32_t b = 0, e = 0;
+    bool full = false;
     if (v < n_cols) {
       const unsigned long long vv = vis[v];
+      full = vv == all_roots;
       nw = vv & ~prev[v];
       if (nw) {
         prev[v] = vv;
@@ -273,16 +310,23 @@ __global__ void __launch_bounds__(kMsBlock) ms_levelgen_kernel(MsState *__restri
       if (hist) hist[v] = nw;
     }
     any |= nw != 0;
+    // hub ids every root has reached (warps cover 32 aligned ids)
+    if (hub_words) {
+      const uint32_t fm = __ballot_sync(kFull, full);
+      if (lane == 0 && (v >> 5) < hub_words) hubfull[v >> 5] = fm;
+    }
     if (!hist) {  // past the history: one root row at a time
+      // rows are in original ids
+      const uint32_t ov = (nw && moved && ((moved[v >> 5] >> (v & 31u)) & 1u)) ? perm[v] : v;
       const uint32_t u_lo = __reduce_or_sync(kFull, (uint32_t)nw);
       const uint32_t u_hi = __reduce_or_sync(kFull, (uint32_t)(nw >> 32));
       for (uint32_t m = u_lo; m; m &= m - 1u) {
         const uint32_t j = __ffs(m) - 1u;
-        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + v] = (int32_t)L;
+        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + ov] = (int32_t)L;
       }
       for (uint32_t m = u_hi; m; m &= m - 1u) {
         const uint32_t j = 32u + __ffs(m) - 1u;
-        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + v] = (int32_t)L;
+        if ((nw >> j) & 1ull) level[(size_t)j * n_cols + ov] = (int32_t)L;
       }
     }
     const uint32_t deg = e - b;
@@ -402,9 +446,13 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
   unsigned long long acc_lo = 0, acc_hi = 0;  // degree sums of roots lane, 32 + lane
   unsigned long long common = 0;              // degree sums of vertices every root reached
   const uint64_t stride = (uint64_t)gridDim.x * kMsBlock;
+  const uint32_t *__restrict__ pinv = st->pinv;
+  const uint32_t *__restrict__ moved = st->moved;
   for (uint64_t t0 = (uint64_t)blockIdx.x * kMsBlock + warp * 32u; t0 < n; t0 += stride) {
-    const uint32_t v = (uint32_t)t0 + lane;
-    const bool in = v < n;
+    const uint32_t ov = (uint32_t)t0 + lane;  // original id: the row entry written
+    const bool in = ov < n;
+    // internal id whose masks and degree belong to it (moved ids only differ)
+    const uint32_t v = (in && moved && ((moved[ov >> 5] >> (ov & 31u)) & 1u)) ? pinv[ov] : ov;
     // this step's loads are issued together: the mask and degree for the
     // edge counts, and history levels 0 .. 7 (8 .. 15 after them, if the
     // search went that deep)
@@ -435,10 +483,10 @@ __global__ void __launch_bounds__(kMsBlock, 4) ms_expand_kernel(MsState *__restr
           }
         }
       }
-      ms_store_rows<0>(level, n, v, in, nl, (uint32_t)r, (uint32_t)p0, (uint32_t)p1,
+      ms_store_rows<0>(level, n, ov, in, nl, (uint32_t)r, (uint32_t)p0, (uint32_t)p1,
                        (uint32_t)p2, (uint32_t)p3);
       if (nl > 32)
-        ms_store_rows<1>(level + (size_t)32 * n, n, v, in, nl, (uint32_t)(r >> 32),
+        ms_store_rows<1>(level + (size_t)32 * n, n, ov, in, nl, (uint32_t)(r >> 32),
                          (uint32_t)(p0 >> 32), (uint32_t)(p1 >> 32), (uint32_t)(p2 >> 32),
                          (uint32_t)(p3 >> 32));
     }
@@ -500,6 +548,9 @@ struct MsWorkspace {
   int grid_ex = 0, grid_lg = 0, grid_xp = 0;
   int32_t *rows = nullptr;  // one pass of level rows for bfs_run_batch_host
   size_t clear_bytes = 0;  // visited and prev masks, history level 0
+  uint32_t *hubfull = nullptr;  // g->words words
+  size_t hub_bytes = 0;    // explore's dynamic shared memory (the hub layout's prefix)
+  uint32_t hub_gen = 0;    // the handle's layout generation this workspace copied
 };
 
 namespace bfsgb {
@@ -514,6 +565,7 @@ void free_msbfs(bfs_graph *g) {
   cudaFree(w->mem);
   cudaFree(w->d_st);
   cudaFree(w->rows);
+  cudaFree(w->hubfull);
   if (w->h_st) cudaFreeHost(w->h_st);
   delete w;
   g->ms = nullptr;
@@ -530,9 +582,17 @@ void free_msbfs(bfs_graph *g) {
   } while (0)
 
 static bfs_status ms_setup(bfs_graph *g) {
+  bfs_status hrc = ensure_hub(g);
+  if (hrc != BFS_OK) return hrc;
+  // the template and the graph below copy the layout's arrays and bake in its
+  // shared-memory size: a workspace built for another layout is rebuilt
+  const size_t hub_bytes = g->hub ? (size_t)g->hub->vertices / 8 : 0;
+  if (g->ms && g->ms->hub_gen != g->hub_gen) free_msbfs(g);
   if (g->ms) return BFS_OK;
   MsWorkspace *w = new MsWorkspace();
   g->ms = w;
+  w->hub_bytes = hub_bytes;
+  w->hub_gen = g->hub_gen;
   const size_t n = g->n_cols, nr = std::max<uint32_t>(g->n_rows, 1);
   auto al = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t b64 = al(n * 8), q4 = al(nr * 4), qp4 = al((nr + 1) * 4), q8 = al(nr * 8);
@@ -549,6 +609,21 @@ static bfs_status ms_setup(bfs_graph *g) {
   s.inds = g->inds;
   s.n_rows = g->n_rows;
   s.n_cols = g->n_cols;
+  if (g->hub) {
+    MK(dev_malloc(&w->hubfull, sizeof(uint32_t) * (size_t)g->words));
+    s.indptr = g->hub->indptr;
+    s.inds = g->hub->inds;
+    s.perm = g->hub->perm;
+    s.pinv = g->hub->pinv;
+    s.moved = g->hub->moved;
+    s.hubfull = w->hubfull;
+    s.hub_words = g->hub->vertices / 32u;
+    s.hub_min_edges = g->hub_min_edges ? g->hub_min_edges
+                                       : std::max<uint32_t>(kHubMinEdges, 2u * g->hub->vertices);
+    if (hub_bytes > 48 * 1024)
+      MK(cudaFuncSetAttribute((const void *)ms_explore_kernel,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hub_bytes));
+  }
   s.vis = (unsigned long long *)p; p += b64;
   s.prev = (unsigned long long *)p; p += b64;
   s.hist = (unsigned long long *)p; p += kHistLevels * b64;
@@ -561,7 +636,7 @@ static bfs_status ms_setup(bfs_graph *g) {
   w->clear_bytes = 3 * b64;  // vis, prev, hist[0] are contiguous
   int occ_ex = 0, occ_lg = 0, occ_xp = 0;
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, (const void *)ms_explore_kernel,
-                                                   kMsBlock, 0));
+                                                   kMsBlock, hub_bytes));
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, (const void *)ms_levelgen_kernel,
                                                    kMsBlock, 0));
   MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_xp, (const void *)ms_expand_kernel,
@@ -586,6 +661,16 @@ static bfs_status ms_setup(bfs_graph *g) {
   mp.height = 1;
   cudaGraphNode_t n_ms, n_init, n_while, n_ex, n_lg, n_xp, n_xf;
   MK(cudaGraphAddMemsetNode(&n_ms, w->graph, nullptr, 0, &mp));
+  cudaGraphNode_t init_deps[2] = {n_ms, nullptr};
+  size_t n_init_deps = 1;
+  if (w->hubfull) {
+    // a pass starts with no hub known to be reached by every root
+    cudaMemsetParams hp = mp;
+    hp.dst = w->hubfull;
+    hp.width = g->words;
+    MK(cudaGraphAddMemsetNode(&init_deps[1], w->graph, nullptr, 0, &hp));
+    n_init_deps = 2;
+  }
   cudaKernelNodeParams kp;
   std::memset(&kp, 0, sizeof(kp));
   void *init_args[] = {&st, &cond_arg, &one};
@@ -593,7 +678,7 @@ static bfs_status ms_setup(bfs_graph *g) {
   kp.gridDim = dim3(1);
   kp.blockDim = dim3(kLanes);
   kp.kernelParams = init_args;
-  MK(cudaGraphAddKernelNode(&n_init, w->graph, &n_ms, 1, &kp));
+  MK(cudaGraphAddKernelNode(&n_init, w->graph, init_deps, n_init_deps, &kp));
   alignas(cudaGraphNodeParams) unsigned char wbuf[sizeof(cudaGraphNodeParams)] = {};
   cudaGraphNodeParams &wp = *reinterpret_cast<cudaGraphNodeParams *>(wbuf);
   wp.type = cudaGraphNodeTypeConditional;
@@ -606,8 +691,10 @@ static bfs_status ms_setup(bfs_graph *g) {
   kp.func = (void *)ms_explore_kernel;
   kp.gridDim = dim3(w->grid_ex);
   kp.blockDim = dim3(kMsBlock);
+  kp.sharedMemBytes = (unsigned)hub_bytes;
   kp.kernelParams = ex_args;
   MK(cudaGraphAddKernelNode(&n_ex, body, nullptr, 0, &kp));
+  kp.sharedMemBytes = 0;
   void *lg_args[] = {&st, &cond_arg, &one};
   kp.func = (void *)ms_levelgen_kernel;
   kp.gridDim = dim3(w->grid_lg);
@@ -636,6 +723,7 @@ static bfs_status ms_pass_host(bfs_graph *g, MsWorkspace *w) {
   unsigned long long no_cond = 0;
   int zero = 0;
   MK(cudaMemsetAsync(w->mem, 0, w->clear_bytes, s));
+  if (w->hubfull) MK(cudaMemsetAsync(w->hubfull, 0, sizeof(uint32_t) * g->words, s));
   ms_init_kernel<<<1, kLanes, 0, s>>>(st, no_cond, zero);
   MK(cudaGetLastError());
   uint32_t *h_F = &w->h_st->F;
@@ -643,7 +731,7 @@ static bfs_status ms_pass_host(bfs_graph *g, MsWorkspace *w) {
     MK(cudaMemcpyAsync(h_F, &st->F, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     MK(cudaStreamSynchronize(s));
     if (*h_F == 0) break;
-    ms_explore_kernel<<<w->grid_ex, kMsBlock, 0, s>>>(st);
+    ms_explore_kernel<<<w->grid_ex, kMsBlock, w->hub_bytes, s>>>(st);
     MK(cudaGetLastError());
     ms_levelgen_kernel<<<w->grid_lg, kMsBlock, 0, s>>>(st, no_cond, zero);
     MK(cudaGetLastError());

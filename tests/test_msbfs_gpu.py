@@ -126,3 +126,65 @@ def test_batch_into_host_arrays(B, O):
     ec3, _ = dg.run_batch(roots, out.data_ptr())
     assert np.array_equal(out.cpu().numpy(), lv) and np.array_equal(ec3, ec)
     dg.free()
+
+
+@pytest.mark.parametrize("K,min_edges", [(1024, 1), (1 << 14, 0)])
+def test_hub_layout_batches(B, O, K, min_edges):
+    """Batches on the relabelled graph of the hub layout: roots mapped in,
+    rows written in original ids, and (min_edges = 1) the shared-memory
+    bitmap of hubs every root has reached skipping mask probes on every
+    level; a later change of layout rebuilds the batch workspace."""
+    torch = torch_cuda()
+    g = B.gen_rmat(16, 16, seed=14)
+    dg = B.Graph.upload(g)
+    roots = B.sample_roots(g, 96, 14)
+    ref, rec = O.oracle_bfs_many(g.indptr, g.inds, roots)
+    out = torch.empty((len(roots), g.n_cols), dtype=torch.int32, device="cuda")
+    for hub in (K, 0, K):
+        dg.hub_configure(hub, min_edges=min_edges)
+        assert dg.hub_info()[1] == (hub > 0)
+        for loop in ("graph", "host"):
+            out.fill_(7)
+            ec, st = dg.run_batch(roots, out.data_ptr(), loop=loop)
+            assert np.array_equal(out.cpu().numpy(), ref), (hub, loop)
+            assert np.array_equal(ec, rec), (hub, loop)
+    dg.free()
+
+
+def test_hub_layout_batches_past_the_history(B, O):
+    """A star (a hub with 3000 leaves) with a 120-vertex chain hanging off it:
+    relabelled (the hub takes half the edge endpoints) and deeper than the
+    16-level history, so the deeper levels are written straight into the rows
+    through the id map."""
+    torch = torch_cuda()
+    leaves, chain = 3000, 120
+    n = 1 + leaves + chain
+    src, dst = [], []
+    for v in range(1, leaves + 1):
+        src += [0, v]
+        dst += [v, 0]
+    prev = leaves
+    for v in range(leaves + 1, n):
+        src += [prev, v]
+        dst += [v, prev]
+        prev = v
+    src, dst = np.array(src), np.array(dst)
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    indptr = np.zeros(n + 1, np.uint32)
+    np.add.at(indptr, src + 1, 1)
+    indptr = np.cumsum(indptr).astype(np.uint32)
+    g = B.Csc(indptr, dst.astype(np.uint32), n, n)
+    dg = B.Graph.upload(g)
+    dg.hub_configure(128, min_edges=1)
+    assert dg.hub_info()[:2] == (128, True)
+    roots = np.array([0, 5, leaves, leaves + 7, n - 1] + list(range(10, 80)), np.uint32)
+    ref, rec = O.oracle_bfs_many(g.indptr, g.inds, roots)
+    assert ref.max() > 16
+    out = torch.empty((len(roots), n), dtype=torch.int32, device="cuda")
+    for loop in ("graph", "host"):
+        out.fill_(7)
+        ec, _ = dg.run_batch(roots, out.data_ptr(), loop=loop)
+        assert np.array_equal(out.cpu().numpy(), ref), loop
+        assert np.array_equal(ec, rec), loop
+    dg.free()

@@ -34,12 +34,12 @@
 //
 // With the graph handle's hub layout (hub_layout.cu) the batch runs on the
 // relabelled graph, whose internal ids 0 .. K-1 are the K highest in-degree
-// vertices: level generation also writes a bitmap of the hub ids every root
-// of the pass has reached (hubfull), explore copies it into shared memory on
-// large levels and skips the 8-byte mask probe of those targets -- on
-// power-law graphs most edges of the later levels point at them, and the
-// mask array is larger than L2, so each probe skipped is a DRAM sector
-// saved.  Rows are written in original ids (expand reads the internal state
+// vertices: level generation also writes a bitmap of the first (at most
+// kMsHubMax) hub ids every root of the pass has reached (hubfull), explore
+// copies it into shared memory on large levels and skips the 8-byte mask
+// probe of those targets -- on power-law graphs many edges of the later
+// levels point at them, and the mask array is larger than L2, so each probe
+// skipped is a DRAM sector saved.  Rows are written in original ids (expand reads the internal state
 // through pinv).
 #include <cuda_runtime.h>
 
@@ -63,6 +63,12 @@ constexpr int kMsU = 4;
 constexpr uint32_t kMsChunk = 32u * kMsU * 4u;
 // Levels kept as per-vertex root masks before the rows are written.
 constexpr uint32_t kHistLevels = 16;
+// Largest hub prefix the batched explore filters on (vertices): six blocks per
+// SM each hold a copy, and every byte of it is taken from the L1 capacity the
+// mask and queue loads need (RMAT-25 64-root pass: 24.5 ms without a filter,
+// 23.6 ms with 32 K, 36.6 ms with 256 K).  The layout is in degree order, so
+// its first 32 K ids are the top hubs whatever its own size.
+constexpr uint32_t kMsHubMax = 1u << 15;
 
 struct MsState {
   const uint32_t *indptr;
@@ -586,7 +592,8 @@ static bfs_status ms_setup(bfs_graph *g) {
   if (hrc != BFS_OK) return hrc;
   // the template and the graph below copy the layout's arrays and bake in its
   // shared-memory size: a workspace built for another layout is rebuilt
-  const size_t hub_bytes = g->hub ? (size_t)g->hub->vertices / 8 : 0;
+  const uint32_t ms_hub = g->hub ? std::min<uint32_t>(g->hub->vertices, kMsHubMax) : 0u;
+  const size_t hub_bytes = (size_t)ms_hub / 8;
   if (g->ms && g->ms->hub_gen != g->hub_gen) free_msbfs(g);
   if (g->ms) return BFS_OK;
   MsWorkspace *w = new MsWorkspace();
@@ -617,9 +624,9 @@ static bfs_status ms_setup(bfs_graph *g) {
     s.pinv = g->hub->pinv;
     s.moved = g->hub->moved;
     s.hubfull = w->hubfull;
-    s.hub_words = g->hub->vertices / 32u;
+    s.hub_words = ms_hub / 32u;
     s.hub_min_edges = g->hub_min_edges ? g->hub_min_edges
-                                       : std::max<uint32_t>(kHubMinEdges, 2u * g->hub->vertices);
+                                       : std::max<uint32_t>(kHubMinEdges, 2u * ms_hub);
     if (hub_bytes > 48 * 1024)
       MK(cudaFuncSetAttribute((const void *)ms_explore_kernel,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hub_bytes));

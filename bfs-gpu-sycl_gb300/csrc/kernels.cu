@@ -859,6 +859,13 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   // reached-vertex count: one atomic per block (reached is warp-uniform)
   if (lane == 0) s_reached[warp] = reached;
   __syncthreads();
+  // fused scheduler (learned runs): every block copies the model into its
+  // (now unused) vertex-list buffer while thread 0 takes the block's ticket,
+  // so that the last block -- which picks the next level's arm -- holds it
+  // by the time it knows it is last.  Thread 0 stays out of the copy: its
+  // fence would otherwise wait for its share of the loads.
+  const float *w = st->sched_w;
+  float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
   if (threadIdx.x == 0) {
     uint32_t t = 0;
     for (int i = 0; i < NW; i++) t += s_reached[i];
@@ -866,22 +873,16 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     __threadfence();
     const uint32_t ticket = atomicAdd(&st->done_blocks, 1u);
     s_last = (ticket == gridDim.x - 1);
+  } else if (w != nullptr) {
+    stage_weights(s_w, w, 1u);
   }
   __syncthreads();
   if (s_last) {  // uniform over the block
-    // fused scheduler: the arm of the level just generated, for the
-    // explore_any launch of the next loop iteration.  The block copies the
-    // model into the (now unused) vertex-list buffer while thread 0 closes
-    // the level.
-    // (thread 0 stays out of the copy: its fence before closing the level
-    // would otherwise wait for its share of the model's loads)
-    const float *w = st->sched_w;
-    float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
+    // the arm of the level just generated, for the explore_any launch of
+    // the next loop iteration
     if (threadIdx.x == 0) {
       __threadfence();
       s_ctr = finish_level(st, cond, use_cond);
-    } else if (w != nullptr) {
-      stage_weights(s_w, w, 1u);
     }
     __syncthreads();
     if (w != nullptr && warp == 0) fused_sched_pick(st, s_ctr, s_w);

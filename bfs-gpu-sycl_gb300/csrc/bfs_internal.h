@@ -87,6 +87,9 @@ BFS_HD uint32_t hash_to_range(uint64_t h, uint32_t n) {
 }
 
 // ---- device state of the level loop ---------------------------------------
+constexpr uint8_t kLv8Unvisited = 0xFF;
+constexpr uint8_t kLv8Deep = 0xFE;
+
 struct BfsDevState {
   // graph
   const uint32_t *indptr;
@@ -105,8 +108,15 @@ struct BfsDevState {
   uint32_t *qd[2];
   uint32_t *qc[2];
   uint32_t *qv[2];
-  int32_t *level;
+  int32_t *level;        // output, original ids; written at the end of the BFS
+                         // (level_out_kernel), during it only for deep levels
   int32_t *parent;       // may be null
+  // working levels, one byte per internal id (words * 32 bytes): kLv8Unvisited,
+  // kLv8Deep (the level is >= kLv8Deep and already in `level`), else the
+  // level.  Small enough to stay in L2, and written a whole 32-byte sector
+  // (one bitmap word) at a time, where 4-byte stores into the output array
+  // would each make L2 fetch the rest of their sector from DRAM.
+  uint8_t *lv8;
   // hub layout (hub_layout.cu): with a relabelled graph, indptr/inds above are
   // the relabelled CSC and the kernels work on internal ids; levels and
   // parents are written in original ids.  Null: identity.

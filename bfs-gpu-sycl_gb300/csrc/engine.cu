@@ -116,12 +116,14 @@ static bfs_status setup_workspace(bfs_graph *g) {
   CK(cudaEventCreate(&g->ev1));
   for (auto &e : g->lvl_ev) CK(cudaEventCreate(&e));
   g->words = (uint32_t)align_up(((size_t)g->n_cols + 31) / 32, 32);
-  // one allocation: bitmaps (vis, prev), three queue arrays x 2, record arrays
+  // one allocation: bitmaps (vis, prev), working levels (one byte per id),
+  // four queue arrays x 2, record arrays
   const size_t bm = align_up((size_t)g->words * 4, 256);
+  const size_t l8 = align_up((size_t)g->words * 32, 256);
   const size_t nq = std::max<size_t>(g->n_rows, 1);
   const size_t q4 = align_up(nq * 4, 256), qp4 = align_up((nq + 1) * 4, 256);
   const size_t rec = align_up((size_t)BFS_MAX_RECORDED_LEVELS * 4, 256);
-  g->ws_bytes = 2 * bm + 2 * (3 * q4 + qp4) + 4 * rec;
+  g->ws_bytes = 2 * bm + l8 + 2 * (3 * q4 + qp4) + 4 * rec;
   CK(dev_malloc(&g->ws, g->ws_bytes));
   char *p = (char *)g->ws;
   BfsDevState &s = g->tmpl;
@@ -135,6 +137,7 @@ static bfs_status setup_workspace(bfs_graph *g) {
   s.words = g->words;
   s.vis = (uint32_t *)p; p += bm;
   s.prev = (uint32_t *)p; p += bm;
+  s.lv8 = (uint8_t *)p; p += l8;
   for (int b = 0; b < 2; b++) {
     s.qb[b] = (uint32_t *)p; p += q4;
     s.qd[b] = (uint32_t *)p; p += q4;
@@ -165,10 +168,14 @@ static bfs_status setup_workspace(bfs_graph *g) {
                                                      kAnyBlock, 0));
     g->occ_any[u] = std::max(occ, 1);
   }
-  int occ_lg = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
-                                                   kLevelgenBlock, 0));
-  g->lg_grid = g->num_sms * std::max(occ_lg, 1);
+  for (int par = 0; par < 2; par++) {
+    const void *fn = levelgen_kernel_fn(par != 0);
+    const size_t smem = levelgen_smem(par != 0);
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ_lg = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, fn, kLevelgenBlock, smem));
+    g->lg_grid[par] = g->num_sms * std::max(occ_lg, 1);
+  }
   // explore_any takes the hub prefix in dynamic shared memory, up to what
   // the device allows a block beside the kernel's own static arrays
   size_t static_max = 0;
@@ -403,6 +410,9 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   wp.conditional.size = 1;
   CK(cudaGraphAddNode(&n_while, graph, &n_init, nullptr, 1, &wp));
   cudaGraph_t body = wp.conditional.phGraph_out[0];
+  cudaGraphNode_t n_out;
+  CK(add_kernel(graph, &n_out, &n_while, 1, level_out_kernel_fn(), g->num_sms * 8, 256,
+                fill_args));
 
   void *ex_args[] = {&st};
   int arm_arg = arm;  // < 0: the scheduler's arm in st->arm
@@ -416,8 +426,9 @@ static bfs_status build_loop_graph(bfs_graph *g, int arm, int sm_factor, int ipt
   }
   set_window(g, n_explore);
   void *lg_args[] = {&st, &cond_arg, &one};
-  CK(add_kernel(body, &n_lg, &n_explore, 1, levelgen_kernel_fn(), g->lg_grid, kLevelgenBlock,
-                lg_args));
+  CK(add_kernel(body, &n_lg, &n_explore, 1, levelgen_kernel_fn(g->run_parents),
+                g->lg_grid[g->run_parents], kLevelgenBlock, lg_args,
+                levelgen_smem(g->run_parents)));
   set_window(g, n_lg);
   CK(cudaGraphInstantiate(&ge->exec, graph, 0));
   return BFS_OK;
@@ -498,13 +509,15 @@ static bfs_status host_loop(bfs_graph *g, int arm_fixed, int sm_factor, int ipt,
     if (prof) CK(cudaEventRecord(g->lvl_ev[1], g->stream));
     if (timer && timer->after) timer->after(timer->ctx, g, level, arm);
     void *lg_args[] = {&st, &no_cond, &zero};
-    CK(cudaLaunchKernel(levelgen_kernel_fn(), dim3(g->lg_grid), dim3(kLevelgenBlock), lg_args, 0,
-                        g->stream));
+    CK(cudaLaunchKernel(levelgen_kernel_fn(g->run_parents), dim3(g->lg_grid[g->run_parents]),
+                        dim3(kLevelgenBlock), lg_args, levelgen_smem(g->run_parents), g->stream));
     if (prof) CK(cudaEventRecord(g->lvl_ev[2], g->stream));
     launches += 2;
     if (level < BFS_MAX_RECORDED_LEVELS) g->host_arms[level] = arm;
   }
-  g->host_launches = launches;
+  CK(cudaLaunchKernel(level_out_kernel_fn(), dim3(g->num_sms * 8), dim3(256), fill_args, 0,
+                      g->stream));
+  g->host_launches = launches + 1;
   return BFS_OK;
 }
 

@@ -82,7 +82,7 @@ struct bfs_graph {
   float *prof_gen = nullptr;
   int occ[2][bfsgb::kNumArms] = {};  // blocks per SM, [ipt == 8][arm]
   int occ_any[2] = {};                // blocks per SM of explore_any, [ipt == 8]
-  int lg_grid = 0;
+  int lg_grid[2] = {0, 0};  // level generation, without / with parents
   bool l2_pinned = false;
   bool use_l2_pin = true;
   bool run_parents = false;  // current run records parents

@@ -19,18 +19,23 @@
 //             with a plain load and only then claims it with atomicOr, instead
 //             of byte masks.
 //   levelgen  scans the bitmap words (n/32, not n bytes): new = vis & ~prev.
-//             Blocks claim spans of words from a counter; each warp lists its
-//             words' new vertices in shared memory, writes their levels and
-//             loads their degrees 32 at a time, and one atomic per block and
-//             span reserves the queue tail.  The atomic adds (count << 32 |
-//             degree sum), so every entry also receives the exclusive prefix
-//             of degrees in queue order: the grid-wide scan that GLB needs
-//             comes out of the same atomic.  Zero-degree vertices and vertices
-//             >= n_rows get their level but are not queued (they would expand
-//             nothing; run_bfs_cpu.hpp:31 never expands tid >= numRows).
+//             Blocks claim spans of words from a counter, write the new
+//             levels a bitmap word (one 32-byte sector of one-byte working
+//             levels) at a time, and list each span's new vertices in shared
+//             memory; warps take equal shares of the list and load degrees
+//             32 at a time, and one atomic per block and span reserves the
+//             queue tail.  The atomic adds (count << 32 | chunk count), so
+//             every entry also receives the exclusive prefix of its 16-byte
+//             edge chunks in queue order: the grid-wide scan that GLB needs
+//             comes out of the same atomic.  Zero-degree vertices and
+//             vertices >= n_rows get their level but are not queued (they
+//             would expand nothing; run_bfs_cpu.hpp:31 never expands
+//             tid >= numRows).
 //   finish    the last level-generation block swaps the queues, accumulates
 //             edgesCount and, in the CUDA-graph loop, sets the while-node
 //             condition, so no host round trip happens between levels.
+//   output    after the last level one pass writes the int32 levels (original
+//             ids, -1 for unvisited) from the working levels.
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -78,31 +83,80 @@ __device__ __forceinline__ uint32_t round_owner(uint32_t cur, uint32_t bnd,
 // ---- fill / init --------------------------------------------------------------
 
 __global__ void fill_kernel(BfsDevState *st) {
-  int32_t *level = st->level, *parent = st->parent;
+  int32_t *parent = st->parent;
   const uint32_t n = st->n_cols;
   const uint32_t stride = gridDim.x * blockDim.x;
-  // int4 stores for the body when both buffers are 16-byte aligned
-  const bool vec = ((reinterpret_cast<uintptr_t>(level) |
-                     reinterpret_cast<uintptr_t>(parent)) & 15u) == 0;
-  const uint32_t n4 = vec ? (n >> 2) : 0u;
-  int4 neg = make_int4(-1, -1, -1, -1);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-    reinterpret_cast<int4 *>(level)[i] = neg;
-    if (parent) reinterpret_cast<int4 *>(parent)[i] = neg;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  // parents to -1 (int4 stores for the body when the buffer is 16-byte
+  // aligned); levels need no fill: level_out_kernel writes every entry
+  if (parent) {
+    const uint32_t n4 = (reinterpret_cast<uintptr_t>(parent) & 15u) == 0 ? (n >> 2) : 0u;
+    const int4 neg = make_int4(-1, -1, -1, -1);
+    for (uint32_t i = tid; i < n4; i += stride) reinterpret_cast<int4 *>(parent)[i] = neg;
+    for (uint32_t i = (n4 << 2) + tid; i < n; i += stride) parent[i] = -1;
   }
-  for (uint32_t i = (n4 << 2) + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    level[i] = -1;
-    if (parent) parent[i] = -1;
-  }
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < st->rec_cap; i += stride)
-    st->rec_ran[i] = -1;
-  // cleared bitmaps: kernel stores rather than a memset, so that a BFS uses
-  // no copy engine between its start and its final state read (words is a
-  // multiple of 32 and both bitmaps are 16-byte aligned)
+  for (uint32_t i = tid; i < st->rec_cap; i += stride) st->rec_ran[i] = -1;
+  // cleared bitmaps and unvisited working levels: kernel stores rather than
+  // a memset, so that a BFS uses no copy engine between its start and its
+  // final state read (words is a multiple of 32, the bitmaps and the
+  // working levels -- 32 bytes per word -- are 16-byte aligned)
   const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (st->words >> 2); i += stride) {
+  for (uint32_t i = tid; i < (st->words >> 2); i += stride) {
     reinterpret_cast<uint4 *>(st->vis)[i] = zero;
     reinterpret_cast<uint4 *>(st->prev)[i] = zero;
+  }
+  const uint4 unvisited = make_uint4(~0u, ~0u, ~0u, ~0u);
+  for (uint32_t i = tid; i < st->words * 2u; i += stride)
+    reinterpret_cast<uint4 *>(st->lv8)[i] = unvisited;
+}
+
+__device__ __forceinline__ int32_t output_level(uint32_t c, const int32_t *level, uint32_t u) {
+  return c == kLv8Unvisited ? -1 : c == kLv8Deep ? level[u] : (int32_t)c;
+}
+
+__device__ __forceinline__ int4 output_levels4(uint32_t c4, const int32_t *level, uint32_t u) {
+  return make_int4(output_level(c4 & 0xFFu, level, u), output_level((c4 >> 8) & 0xFFu, level, u + 1),
+                   output_level((c4 >> 16) & 0xFFu, level, u + 2),
+                   output_level(c4 >> 24, level, u + 3));
+}
+
+// Output levels, original id u from the working level of its internal id:
+// every entry of `level` is written (-1 for unvisited), deep levels (written
+// during the BFS) are kept.  A thread takes 16 ids per step: one 16-byte
+// load of working levels and four 16-byte stores when none of them is
+// relabelled.  A relabelled id u is moved exactly when bit u of the moved
+// bitmap is set (perm[u] != u iff pinv[u] != u); a group with moved ids
+// gathers each one's working level through pinv.
+__global__ void level_out_kernel(BfsDevState *st) {
+  int32_t *level = st->level;
+  const uint8_t *lv8 = st->lv8;
+  const uint32_t *moved = st->moved, *pinv = st->pinv;
+  const uint32_t n = st->n_cols;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n16 = (reinterpret_cast<uintptr_t>(level) & 15u) == 0 ? (n >> 4) : 0u;
+  for (uint32_t i = tid; i < n16; i += stride) {
+    const uint32_t u = i << 4;
+    const uint32_t mb = moved ? (moved[u >> 5] >> (u & 31u)) & 0xFFFFu : 0u;
+    int4 *dst = reinterpret_cast<int4 *>(level + u);
+    if (mb == 0) {
+      const uint4 c = reinterpret_cast<const uint4 *>(lv8)[i];
+      dst[0] = output_levels4(c.x, level, u);
+      dst[1] = output_levels4(c.y, level, u + 4);
+      dst[2] = output_levels4(c.z, level, u + 8);
+      dst[3] = output_levels4(c.w, level, u + 12);
+    } else {
+      uint32_t c[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (uint32_t k = 0; k < 16; k++)
+        c[k >> 2] |= (uint32_t)lv8[((mb >> k) & 1u) ? pinv[u + k] : u + k] << (8u * (k & 3u));
+#pragma unroll
+      for (uint32_t j = 0; j < 4; j++) dst[j] = output_levels4(c[j], level, u + 4 * j);
+    }
+  }
+  for (uint32_t u = (n16 << 4) + tid; u < n; u += stride) {
+    const bool mv = moved && ((moved[u >> 5] >> (u & 31u)) & 1u);
+    level[u] = output_level(lv8[mv ? pinv[u] : u], level, u);
   }
 }
 
@@ -163,7 +217,7 @@ __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_con
   const uint32_t ri = st->pinv ? st->pinv[r] : r;  // internal id
   st->vis[ri >> 5] |= 1u << (ri & 31u);
   st->prev[ri >> 5] |= 1u << (ri & 31u);
-  st->level[r] = 0;
+  st->lv8[ri] = 0;
   if (st->parent) st->parent[r] = (int32_t)r;
   const bool expanded = ri < st->n_rows;  // run_bfs_cpu.hpp:31
   uint32_t b = 0, e = 0;
@@ -198,7 +252,7 @@ __device__ void init_state(BfsDevState *st, unsigned long long cond, int use_con
   st->done_blocks = 0;
   st->lg_cursor = 0;
   st->error = 0;
-  st->launches = 2;
+  st->launches = 3;  // fill, init and the level output after the loop
   st->arm = st->fixed_arm >= 0 ? st->fixed_arm : 0;
   if (st->rec_cap > 0) {
     st->rec_frontier[0] = st->F;
@@ -683,36 +737,56 @@ __device__ LevelCounters finish_level(BfsDevState *st, unsigned long long cond, 
   return LevelCounters{st->F, ef_new, reached, lvl};
 }
 
-// Level generation.  Blocks claim spans of NW * 32 bitmap words from a
-// counter (the density of new vertices is uneven over the bitmap); warp w of
-// a block owns the w-th group of 32 words of its span.  A warp first lists
-// its group's new vertices (vis & ~prev) in shared memory -- each lane walks
-// its word's set bits -- so that lane l of round r then takes the
-// (32 r + l)-th new vertex with one shared load, and 32 indptr loads are in
-// flight per round whatever the bit layout.  Pass 1 writes levels (in
-// original ids under the hub layout) and counts kept entries, their degrees
-// and their 16-byte chunks; thread 0 reserves the block's queue slots and
-// chunk offsets with one atomic -- slots and the chunk prefix must come from
-// the same atomic, so that the prefix is in slot order -- adds the degrees
-// to the level's edge total and claims the block's next span in the same
-// step; pass 2 re-reads the (now cached) indptr pairs and writes the
-// entries.  Two block barriers per span.
-constexpr int kLgUnroll = 4;
-constexpr int kLgMinBlocks = 5;  // 1280 threads per SM: at most 48 registers
+// Merges new-vertex bits into one 4-byte word of working levels (one byte
+// per vertex): bytes whose bit in the low nibble of `bits` is set take the
+// matching byte of `rep`.  The nibble is spread to bytes by one multiply (its
+// shifted copies land on distinct bit positions, so no carries).
+__device__ __forceinline__ uint32_t merge_levels(uint32_t word, uint32_t bits, uint32_t rep) {
+  const uint32_t m = (((bits & 0xFu) * 0x00204081u) & 0x01010101u) * 0xFFu;
+  return (word & ~m) | (rep & m);
+}
 
-template <int B>
+// Level generation.  Blocks claim spans of B bitmap words (one word per
+// thread) from a counter -- the density of new vertices is uneven over the
+// bitmap.  A block takes the claim of its next span when the current one
+// starts and loads the next span's words while it works on the current one.
+// Each thread writes its word's new levels into the working levels: the
+// word's 32 vertices are one 32-byte sector there, read when the word is
+// seen and written back whole once the block's list is built.  The block
+// lists the span's new vertices (vis & ~prev) in shared memory in vertex
+// order (a block scan of the words' popcounts; each thread walks its word's
+// set bits), then every warp takes an equal share of the list, whatever the
+// bit layout.  Pass 1 loads each entry's indptr pair (kLgUnroll rounds of
+// loads in flight per lane), keeps the entry's offset and degree in shared
+// memory in place of it, and counts kept entries, their degrees and their
+// 16-byte chunks; thread 0 reserves the block's queue slots and chunk
+// offsets with one atomic -- slots and the chunk prefix must come from the
+// same atomic, so that the prefix is in slot order -- and adds the degrees to
+// the level's edge total; pass 2 writes the kept entries from shared memory.
+// Four block barriers per span with new vertices, one per span without.
+constexpr int kLgUnroll = 8;
+constexpr int kLgMinBlocks = 3;  // 768 threads per SM: at most 80 registers
+
+template <int B, bool PAR>
 __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *__restrict__ st,
                                                                    unsigned long long cond,
                                                                    int use_cond) {
   constexpr int NW = B / 32;
-  constexpr uint32_t kSpan = NW * 32u;  // words per block and step
-  static_assert(kSchedParams <= NW * 32 * 32, "the model must fit the list buffer");
-  __shared__ uint32_t s_list[NW][32 * 32];
+  constexpr uint32_t kSpan = B;         // words per block and step
+  constexpr uint32_t kCap = kSpan * 32u;  // list capacity: every vertex of a span
+  static_assert((NW & (NW - 1)) == 0, "warps per block: a power of two");
+  static_assert(kSchedParams <= kCap, "the model must fit the list buffer");
+  // list: entry (vertex id, bit 31 the moved flag), then its indptr offset;
+  // degrees; original ids (parents only)
+  extern __shared__ __align__(16) uint32_t s_dyn[];
+  uint32_t *__restrict__ s_b = s_dyn;
+  uint32_t *__restrict__ s_d = s_dyn + kCap;
+  uint32_t *__restrict__ s_o = s_dyn + 2 * kCap;
+  __shared__ uint32_t s_wc[2][NW];
   __shared__ unsigned long long s_wtot[NW];
   __shared__ uint32_t s_wdeg[NW];
   __shared__ unsigned long long s_base;
   __shared__ uint32_t s_sb[2];
-  __shared__ uint32_t s_reached[NW];
   __shared__ int s_last;
   __shared__ LevelCounters s_ctr;
 
@@ -722,66 +796,116 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   const uint32_t *__restrict__ indptr = st->indptr;
   const uint32_t n_rows = st->n_rows;
   const int32_t lvl_next = (int32_t)st->lvl + 1;
-  int32_t *__restrict__ level = st->level;
+  int32_t *__restrict__ level = st->level;  // deep levels only
+  uint8_t *__restrict__ lv8 = st->lv8;
   const uint32_t nq = st->cur ^ 1u;
   uint32_t *__restrict__ qb = st->qb[nq];
   uint32_t *__restrict__ qd = st->qd[nq];
   uint32_t *__restrict__ qc = st->qc[nq];
   uint32_t *__restrict__ qv = st->qv[nq];
   const uint32_t off = st->inds_off;
-  const uint32_t *__restrict__ perm = st->perm;  // internal -> original (null: identity)
+  const uint32_t *__restrict__ perm = st->perm;    // internal -> original (null: identity)
   const uint32_t *__restrict__ moved = st->moved;  // bit v: perm[v] != v
   // relabelled graphs have fewer than 2^31 vertices: bit 31 of a list entry
   // is then free for the moved flag
   const uint32_t id_mask = moved ? 0x7FFFFFFFu : 0xFFFFFFFFu;
-  const bool want_vid = st->parent != nullptr;   // vertex ids are read for parents only
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t *__restrict__ list = s_list[warp];
-  uint32_t reached = 0;
+  uint32_t reached = 0;  // thread 0's count of the block's new vertices
 
   if (threadIdx.x == 0) s_sb[0] = atomicAdd(&st->lg_cursor, kSpan);
   __syncthreads();
-  for (uint32_t step = 0;; step ^= 1u) {
-    const uint32_t sb = s_sb[step];
-    if (sb >= words) break;
-    const uint32_t w0 = sb + warp * 32u;  // words is a multiple of 32
-    uint32_t tot = 0;
-    if (w0 < words) {
-      const uint32_t vw = V[w0 + lane], pw = P[w0 + lane];
-      uint32_t x = vw & ~pw;
-      if (x) P[w0 + lane] = vw;
-      // under a relabelling, bit 31 of a list entry marks an id whose
-      // original id differs (the only ones that need a perm lookup)
-      const uint32_t mw = (moved && x) ? moved[w0 + lane] : 0u;
-      const uint32_t c = __popc(x);
-      const uint32_t incl = warp_incl_scan(c, lane);
-      tot = __shfl_sync(kFull, incl, 31);
-      uint32_t pos = incl - c;
-      const uint32_t vbase = (w0 + lane) * 32u;
-      __syncwarp();  // the previous span's reads of the list are done
+  uint32_t sb = s_sb[0];
+  // this thread's word of the current span: vis, prev, moved
+  uint32_t vw = 0, pw = 0, mw = 0;
+  if (sb + threadIdx.x < words) {
+    vw = V[sb + threadIdx.x];
+    pw = P[sb + threadIdx.x];
+    if (moved) mw = moved[sb + threadIdx.x];
+  }
+  for (uint32_t step = 0; sb < words; step ^= 1u) {
+    const uint32_t w = sb + threadIdx.x;
+    uint32_t x = vw & ~pw;
+    const uint32_t xn = x, xm = mw;
+    // the word's working levels, merged and written back after the list
+    uint4 *__restrict__ sec = reinterpret_cast<uint4 *>(lv8) + 2u * (size_t)w;
+    uint4 l0 = make_uint4(0u, 0u, 0u, 0u), l1 = l0;
+    if (x) {  // x != 0 only for words < words
+      P[w] = vw;
+      l0 = sec[0];
+      l1 = sec[1];
+    }
+    const uint32_t c = __popc(x);
+    const uint32_t incl = warp_incl_scan(c, lane);
+    if (lane == 31) s_wc[step][warp] = incl;
+    if (threadIdx.x == 0) s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
+    __syncthreads();
+    uint32_t L = 0, woff = 0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) {
+      const uint32_t y = s_wc[step][i];
+      woff += (uint32_t)i < warp ? y : 0u;
+      L += y;
+    }
+    // the next span's words, in flight while this span is worked on
+    sb = s_sb[step ^ 1u];
+    vw = pw = mw = 0;
+    if (sb + threadIdx.x < words) {
+      vw = V[sb + threadIdx.x];
+      pw = P[sb + threadIdx.x];
+      if (moved) mw = moved[sb + threadIdx.x];
+    }
+    if (L == 0) continue;  // uniform over the block
+    reached += L;
+    {
+      uint32_t pos = woff + incl - c;
+      const uint32_t vbase = w * 32u;
       while (x) {
         const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
-        list[pos++] = (vbase + bpos) | (((mw >> bpos) & 1u) << 31);
+        s_b[pos++] = (vbase + bpos) | (((xm >> bpos) & 1u) << 31);
         x &= x - 1u;
       }
-      __syncwarp();
     }
-    reached += tot;
-    // pass 1: levels; kept-entry count, degree and chunk sums of the warp.
-    // kLgUnroll rounds are resolved first so their indptr loads are in flight
-    // together.
-    uint32_t w_cnt = 0, w_deg = 0, w_chk = 0;
-    for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
-      uint32_t b[kLgUnroll], e[kLgUnroll];
+    if (xn) {
+      const uint32_t rep = (lvl_next < (int32_t)kLv8Deep ? (uint32_t)lvl_next : kLv8Deep) *
+                           0x01010101u;
+      l0.x = merge_levels(l0.x, xn, rep);
+      l0.y = merge_levels(l0.y, xn >> 4, rep);
+      l0.z = merge_levels(l0.z, xn >> 8, rep);
+      l0.w = merge_levels(l0.w, xn >> 12, rep);
+      l1.x = merge_levels(l1.x, xn >> 16, rep);
+      l1.y = merge_levels(l1.y, xn >> 20, rep);
+      l1.z = merge_levels(l1.z, xn >> 24, rep);
+      l1.w = merge_levels(l1.w, xn >> 28, rep);
+      sec[0] = l0;
+      sec[1] = l1;
+      if (lvl_next >= (int32_t)kLv8Deep) {
+        // deep level: the level itself goes to the output (original ids)
+        for (uint32_t y = xn; y; y &= y - 1u) {
+          const uint32_t bpos = (uint32_t)(__ffs(y) - 1);
+          const uint32_t v = w * 32u + bpos;
+          level[((xm >> bpos) & 1u) ? perm[v] : v] = lvl_next;
+        }
+      }
+    }
+    __syncthreads();
+    // this warp's share of the list
+    const uint32_t lo = (L * warp) / NW, hi = (L * (warp + 1u)) / NW;
+    // pass 1: indptr pairs (and original ids, for parents) into shared
+    // memory; per-lane kept-entry count, degree and chunk sums.  Every
+    // round's loads are issued before the first use.
+    uint32_t n_cnt = 0, n_deg = 0, n_chk = 0;
+    for (uint32_t t0 = lo; t0 < hi; t0 += 32u * kLgUnroll) {
+      uint32_t b[kLgUnroll], e[kLgUnroll], o[kLgUnroll];
 #pragma unroll
       for (int r = 0; r < kLgUnroll; r++) {
-        const uint32_t t = t0 + 32u * r + lane;
+        const uint32_t i = t0 + 32u * r + lane;
         b[r] = e[r] = 0;
-        if (t < tot) {
-          const uint32_t ent = list[t];
+        o[r] = 0;
+        if (i < hi) {
+          const uint32_t ent = s_b[i];
           const uint32_t v = ent & id_mask;
-          level[(ent & ~id_mask) ? perm[v] : v] = lvl_next;
+          if (PAR) o[r] = (ent & ~id_mask) ? perm[v] : v;
           if (v < n_rows) {
             b[r] = indptr[v];
             e[r] = indptr[v + 1];
@@ -790,86 +914,78 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
       }
 #pragma unroll
       for (int r = 0; r < kLgUnroll; r++) {
+        const uint32_t i = t0 + 32u * r + lane;
         const uint32_t deg = e[r] - b[r];
-        w_cnt += __popc(__ballot_sync(kFull, deg > 0u));
-        w_deg += __reduce_add_sync(kFull, deg);
-        w_chk += __reduce_add_sync(kFull, edge_chunks(b[r], deg, off));
+        if (i < hi) {
+          if (PAR) s_o[i] = o[r];
+          s_b[i] = b[r];
+          s_d[i] = deg;
+        }
+        n_cnt += deg > 0u;
+        n_deg += deg;
+        n_chk += edge_chunks(b[r], deg, off);
       }
     }
-    // block-wide offsets (one atomic per block and step) and the next span
+    n_cnt = __reduce_add_sync(kFull, n_cnt);
+    n_deg = __reduce_add_sync(kFull, n_deg);
+    n_chk = __reduce_add_sync(kFull, n_chk);
     if (lane == 0) {
-      s_wtot[warp] = ((unsigned long long)w_cnt << 32) | w_chk;
-      s_wdeg[warp] = w_deg;
+      s_wtot[warp] = ((unsigned long long)n_cnt << 32) | n_chk;
+      s_wdeg[warp] = n_deg;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned long long run = 0;
       uint32_t deg_sum = 0;
       for (int i = 0; i < NW; i++) {
-        const unsigned long long x = s_wtot[i];
+        const unsigned long long y = s_wtot[i];
         s_wtot[i] = run;
-        run += x;
+        run += y;
         deg_sum += s_wdeg[i];
       }
       s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
       if (deg_sum) atomicAdd(&st->next_edges, deg_sum);  // a total: order does not matter
-      s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
     }
     __syncthreads();
-    if (w_cnt) {
+    if (n_cnt) {
+      // pass 2: the kept entries, in list order
       const unsigned long long wb = s_base + s_wtot[warp];
       uint32_t slot = (uint32_t)(wb >> 32), prefc = (uint32_t)wb;
-      // pass 2: write the kept entries in the same order
-      for (uint32_t t0 = 0; t0 < tot; t0 += 32u * kLgUnroll) {
-        uint32_t vv[kLgUnroll], mf[kLgUnroll], b[kLgUnroll], e[kLgUnroll];
-#pragma unroll
-        for (int r = 0; r < kLgUnroll; r++) {
-          const uint32_t t = t0 + 32u * r + lane;
-          const uint32_t ent = t < tot ? list[t] : kFull;
-          vv[r] = t < tot ? (ent & id_mask) : kFull;
-          mf[r] = t < tot ? (ent & ~id_mask) : 0u;
-          b[r] = e[r] = 0;
-          if (vv[r] < n_rows) {  // kFull >= n_rows
-            b[r] = indptr[vv[r]];
-            e[r] = indptr[vv[r] + 1];
-          }
+      for (uint32_t t0 = lo; t0 < hi; t0 += 32u) {
+        const uint32_t i = t0 + lane;
+        uint32_t b = 0, deg = 0;
+        if (i < hi) {
+          b = s_b[i];
+          deg = s_d[i];
         }
-#pragma unroll
-        for (int r = 0; r < kLgUnroll; r++) {
-          const uint32_t deg = e[r] - b[r];
-          const uint32_t nch = edge_chunks(b[r], deg, off);
-          const uint32_t km = __ballot_sync(kFull, deg > 0u);
-          const uint32_t cincl = warp_incl_scan(nch, lane);
-          if (deg) {
-            const uint32_t sl = slot + __popc(km & lt_mask);
-            qb[sl] = b[r];
-            qd[sl] = deg;
-            qc[sl] = prefc + cincl - nch;
-            if (want_vid) qv[sl] = mf[r] ? perm[vv[r]] : vv[r];
-          }
-          slot += __popc(km);
-          prefc += __shfl_sync(kFull, cincl, 31);
+        const uint32_t nch = edge_chunks(b, deg, off);
+        const uint32_t km = __ballot_sync(kFull, deg > 0u);
+        const uint32_t cincl = warp_incl_scan(nch, lane);
+        if (deg) {
+          const uint32_t sl = slot + __popc(km & lt_mask);
+          qb[sl] = b;
+          qd[sl] = deg;
+          qc[sl] = prefc + cincl - nch;
+          if (PAR) qv[sl] = s_o[i];
         }
+        slot += __popc(km);
+        prefc += __shfl_sync(kFull, cincl, 31);
       }
     }
-    // the list is rewritten only after the next step's first barrier, so
+    // the list is rewritten only after the next span's first barrier, so
     // pass 2 needs no trailing barrier
   }
 
-  // reached-vertex count: one atomic per block (reached is warp-uniform)
-  if (lane == 0) s_reached[warp] = reached;
-  __syncthreads();
   // fused scheduler (learned runs): every block copies the model into its
-  // (now unused) vertex-list buffer while thread 0 takes the block's ticket,
-  // so that the last block -- which picks the next level's arm -- holds it
-  // by the time it knows it is last.  Thread 0 stays out of the copy: its
-  // fence would otherwise wait for its share of the loads.
+  // (now unused) list buffer while thread 0 takes the block's ticket, so
+  // that the last block -- which picks the next level's arm -- holds it by
+  // the time it knows it is last.  Thread 0 stays out of the copy: its fence
+  // would otherwise wait for its share of the loads.
   const float *w = st->sched_w;
-  float *s_w = reinterpret_cast<float *>(&s_list[0][0]);
+  float *s_w = reinterpret_cast<float *>(s_dyn);
+  if (w != nullptr) __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t t = 0;
-    for (int i = 0; i < NW; i++) t += s_reached[i];
-    if (t) atomicAdd(&st->reached, t);
+    if (reached) atomicAdd(&st->reached, reached);
     __threadfence();
     const uint32_t ticket = atomicAdd(&st->done_blocks, 1u);
     s_last = (ticket == gridDim.x - 1);
@@ -1001,9 +1117,16 @@ const void *explore_any_kernel_fn(int ipt, bool parents) {
     return ipt == 8 ? (const void *)explore_any_kernel<8, true> : (const void *)explore_any_kernel<4, true>;
   return ipt == 8 ? (const void *)explore_any_kernel<8, false> : (const void *)explore_any_kernel<4, false>;
 }
-const void *levelgen_kernel_fn() { return (const void *)levelgen_kernel<kLevelgenBlock>; }
+const void *levelgen_kernel_fn(bool parents) {
+  return parents ? (const void *)levelgen_kernel<kLevelgenBlock, true>
+                 : (const void *)levelgen_kernel<kLevelgenBlock, false>;
+}
+size_t levelgen_smem(bool parents) {
+  return (parents ? 3u : 2u) * kLevelgenBlock * 32u * sizeof(uint32_t);
+}
 const void *init_kernel_fn() { return (const void *)init_kernel; }
 const void *fill_kernel_fn() { return (const void *)fill_kernel; }
+const void *level_out_kernel_fn() { return (const void *)level_out_kernel; }
 
 cudaError_t launch_validate(const uint32_t *indptr, const uint32_t *inds, uint32_t n_rows,
                             uint32_t n_cols, uint32_t root, const int32_t *level,

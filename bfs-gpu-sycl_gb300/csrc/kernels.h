@@ -28,10 +28,18 @@ const void *explore_kernel_fn(int arm, int ipt, bool parents);
 // dynamic shared memory of st->hub_words words for GLB levels behind the hub
 // filter (the function's maximum dynamic shared memory must be raised first).
 const void *explore_any_kernel_fn(int ipt, bool parents);
-const void *levelgen_kernel_fn();
+// Level generation: kLevelgenBlock threads, levelgen_smem(parents) bytes of
+// dynamic shared memory (above the default limit: the function's maximum
+// dynamic shared memory must be raised first).
+const void *levelgen_kernel_fn(bool parents);
+size_t levelgen_smem(bool parents);
 const void *init_kernel_fn();
-// fill also clears the visited bitmaps (vis, prev: st->words words each).
+// fill clears the visited bitmaps (vis, prev: st->words words each), marks
+// every working level unvisited and sets parents (when recorded) to -1.
 const void *fill_kernel_fn();
+// Writes the output levels (st->level, every entry) from the working levels;
+// runs once after the level loop.  Arguments (BfsDevState*).
+const void *level_out_kernel_fn();
 // Writes the state st from a host copy with one small kernel.
 cudaError_t launch_seed_state(BfsDevState *st, const BfsDevState &s, cudaStream_t stream);
 

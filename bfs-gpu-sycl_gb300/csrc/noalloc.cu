@@ -60,7 +60,8 @@ constexpr size_t kVisOff = kBadOff + 256;
 constexpr size_t kPrevOff = kVisOff + align256(kWordsMax * 4);
 constexpr size_t kQ4 = align256((size_t)kMaxV * 4);
 constexpr size_t kQp4 = align256(((size_t)kMaxV + 1) * 4);
-constexpr size_t kQOff = kPrevOff + align256(kWordsMax * 4);
+constexpr size_t kLv8Off = kPrevOff + align256(kWordsMax * 4);
+constexpr size_t kQOff = kLv8Off + align256(kWordsMax * 32);
 constexpr size_t kScratchBytes = kQOff + 2 * (3 * kQ4 + kQp4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -97,8 +98,11 @@ bfs_status setup_device(int dev) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ex, explore_kernel_fn(kArm, kIpt, false),
                                                       arm_block(kArm), 0);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(),
-                                                      kLevelgenBlock, 0);
+    e = cudaFuncSetAttribute(levelgen_kernel_fn(false), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)levelgen_smem(false));
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_lg, levelgen_kernel_fn(false),
+                                                      kLevelgenBlock, levelgen_smem(false));
   if (e != cudaSuccess)
     return fail(BFS_ERR_CUDA, std::string("launch geometry: ") + cudaGetErrorString(e));
   g_grid[dev][0] = sms * (occ_ex > 0 ? occ_ex : 1);
@@ -153,6 +157,7 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
   h.root = root;
   h.vis = (uint32_t *)(base + kVisOff);
   h.prev = (uint32_t *)(base + kPrevOff);
+  h.lv8 = base + kLv8Off;
   for (int b = 0; b < 2; b++) {
     unsigned char *q = base + kQOff + (size_t)b * (3 * kQ4 + kQp4);
     h.qb[b] = (uint32_t *)q;
@@ -192,9 +197,10 @@ extern "C" bfs_status bfs_run_device_noalloc(const uint32_t *d_indptr, const uin
     NK(cudaLaunchKernel(explore_kernel_fn(kArm, kIpt, false), dim3(g_grid[dev][0]), dim3(arm_block(kArm)),
                         ex_args, 0, s));
     void *lg_args[] = {&st, &no_cond, &zero};
-    NK(cudaLaunchKernel(levelgen_kernel_fn(), dim3(g_grid[dev][1]), dim3(kLevelgenBlock), lg_args,
-                        0, s));
+    NK(cudaLaunchKernel(levelgen_kernel_fn(false), dim3(g_grid[dev][1]), dim3(kLevelgenBlock),
+                        lg_args, levelgen_smem(false), s));
   }
+  NK(cudaLaunchKernel(level_out_kernel_fn(), dim3(g_grid[dev][1]), dim3(256), fill_args, 0, s));
   uint32_t err = 0;
   unsigned long long edges = 0;
   NK(cudaMemcpyAsync(&err, &st->error, sizeof(err), cudaMemcpyDeviceToHost, s));

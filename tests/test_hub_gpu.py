@@ -207,3 +207,54 @@ def test_hub_configure_rejects_bad_request(B):
     with pytest.raises(B.BfsError):
         dg.hub_configure(-2)
     dg.free()
+
+
+def star_and_path(B, n_leaves=3000, n_path=700, seed=13):
+    """A star (centre of in-degree n_leaves) with a path of n_path vertices
+    hanging off one leaf, ids shuffled: a 128-vertex prefix relabels the
+    centre and scatters moved ids, and the path's levels run past 254."""
+    n = 1 + n_leaves + n_path
+    rng = np.random.default_rng(seed)
+    ids = rng.permutation(n)  # logical vertex -> id
+    c = ids[0]
+    edges = []
+    for k in range(1, n_leaves + 1):
+        edges += [(c, ids[k]), (ids[k], c)]
+    prev = ids[n_leaves]
+    for k in range(n_leaves + 1, n):
+        edges += [(prev, ids[k]), (ids[k], prev)]
+        prev = ids[k]
+    e = np.array(edges, np.int64)
+    order = np.lexsort((e[:, 1], e[:, 0]))
+    e = e[order]
+    indptr = np.zeros(n + 1, np.uint32)
+    indptr[1:] = np.cumsum(np.bincount(e[:, 0], minlength=n))
+    return B.Csc(indptr, e[:, 1].astype(np.uint32)), int(c), int(ids[n - 1])
+
+
+def test_deep_levels_relabelled(B, O):
+    """Levels past the one-byte working range (>= 254) on a relabelled graph:
+    deep levels are written in original ids during the BFS and kept by the
+    output pass; shallow ones come from the working levels through pinv.
+    Output buffers 16-byte aligned and not (the output pass's scalar path)."""
+    torch = torch_cuda()
+    g, centre, tail = star_and_path(B)
+    dg = B.Graph.upload(g)
+    dg.hub_configure(128, min_edges=1)
+    assert dg.hub_info()[:2] == (128, True)
+    buf = torch.empty(g.n_cols + 4, dtype=torch.int32, device="cuda")
+    for r in (centre, tail):
+        ref, ec = O.oracle_bfs(g.indptr, g.inds, r)
+        assert ref.max() > 600
+        for lb, loop in (("glb", "graph"), ("glb", "host"), ("learned", "graph"),
+                         ("llb", "host"), ("slb", "graph")):
+            lv, pa, st = dg.run(r, B.options(lb, 256, loop=loop), parents=True)
+            assert np.array_equal(lv, ref), (r, lb, loop)
+            assert st.edges_count == ec
+            check_tree(g.indptr, g.inds, lv, pa, r)
+        for shift in (0, 1, 3):
+            ptr = buf.data_ptr() + 4 * shift
+            st = dg.run_device(r, ptr, opts=B.options("glb", 256))
+            out = buf[shift:shift + g.n_cols].cpu().numpy()
+            assert np.array_equal(out, ref), (r, shift)
+    dg.free()

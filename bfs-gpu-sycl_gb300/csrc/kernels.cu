@@ -122,39 +122,49 @@ __device__ __forceinline__ int4 output_levels4(uint32_t c4, const int32_t *level
 
 // Output levels, original id u from the working level of its internal id:
 // every entry of `level` is written (-1 for unvisited), deep levels (written
-// during the BFS) are kept.  A thread takes 16 ids per step: one 16-byte
-// load of working levels and four 16-byte stores when none of them is
-// relabelled.  A relabelled id u is moved exactly when bit u of the moved
+// during the BFS) are kept.  Lane l of a warp step takes the 4-id groups
+// g0 + 32 k (k < 4, g0 = 128 x warp + l): each store instruction writes 512
+// contiguous bytes (whole sectors), and the four groups' loads are in flight
+// together.  A relabelled id u is moved exactly when bit u of the moved
 // bitmap is set (perm[u] != u iff pinv[u] != u); a group with moved ids
-// gathers each one's working level through pinv.
+// gathers their working levels through pinv.
 __global__ void level_out_kernel(BfsDevState *st) {
   int32_t *level = st->level;
   const uint8_t *lv8 = st->lv8;
   const uint32_t *moved = st->moved, *pinv = st->pinv;
   const uint32_t n = st->n_cols;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t n16 = (reinterpret_cast<uintptr_t>(level) & 15u) == 0 ? (n >> 4) : 0u;
-  for (uint32_t i = tid; i < n16; i += stride) {
-    const uint32_t u = i << 4;
-    const uint32_t mb = moved ? (moved[u >> 5] >> (u & 31u)) & 0xFFFFu : 0u;
-    int4 *dst = reinterpret_cast<int4 *>(level + u);
-    if (mb == 0) {
-      const uint4 c = reinterpret_cast<const uint4 *>(lv8)[i];
-      dst[0] = output_levels4(c.x, level, u);
-      dst[1] = output_levels4(c.y, level, u + 4);
-      dst[2] = output_levels4(c.z, level, u + 8);
-      dst[3] = output_levels4(c.w, level, u + 12);
-    } else {
-      uint32_t c[4] = {0u, 0u, 0u, 0u};
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t step = gridDim.x * blockDim.x * 4u;  // groups per grid step
+  const uint32_t n4 = (reinterpret_cast<uintptr_t>(level) & 15u) == 0 ? (n >> 2) : 0u;
+  for (uint32_t g0 = gwarp * 128u + lane; g0 < n4; g0 += step) {
+    uint32_t c[4], mb[4];
 #pragma unroll
-      for (uint32_t k = 0; k < 16; k++)
-        c[k >> 2] |= (uint32_t)lv8[((mb >> k) & 1u) ? pinv[u + k] : u + k] << (8u * (k & 3u));
+    for (int k = 0; k < 4; k++) {
+      const uint32_t g = g0 + 32u * k, u = g << 2;
+      c[k] = mb[k] = 0;
+      if (g < n4) {
+        c[k] = reinterpret_cast<const uint32_t *>(lv8)[g];
+        if (moved) mb[k] = (moved[u >> 5] >> (u & 31u)) & 0xFu;
+      }
+    }
 #pragma unroll
-      for (uint32_t j = 0; j < 4; j++) dst[j] = output_levels4(c[j], level, u + 4 * j);
+    for (int k = 0; k < 4; k++) {
+      const uint32_t g = g0 + 32u * k, u = g << 2;
+      if (g < n4) {
+        if (mb[k]) {
+          uint32_t x = 0;
+#pragma unroll
+          for (uint32_t i = 0; i < 4; i++)
+            x |= (uint32_t)lv8[((mb[k] >> i) & 1u) ? pinv[u + i] : u + i] << (8u * i);
+          c[k] = x;
+        }
+        reinterpret_cast<int4 *>(level)[g] = output_levels4(c[k], level, u);
+      }
     }
   }
-  for (uint32_t u = (n16 << 4) + tid; u < n; u += stride) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t u = (n4 << 2) + blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
     const bool mv = moved && ((moved[u >> 5] >> (u & 31u)) & 1u);
     level[u] = output_level(lv8[mv ? pinv[u] : u], level, u);
   }

@@ -772,8 +772,10 @@ __device__ __forceinline__ uint32_t merge_levels(uint32_t word, uint32_t bits, u
 // 16-byte chunks; thread 0 reserves the block's queue slots and chunk
 // offsets with one atomic -- slots and the chunk prefix must come from the
 // same atomic, so that the prefix is in slot order -- and adds the degrees to
-// the level's edge total; pass 2 writes the kept entries from shared memory.
-// Four block barriers per span with new vertices, one per span without.
+// the level's edge total; pass 2 compacts the kept entries in shared memory
+// and writes them in 32-slot windows aligned to 128 bytes, so that the queue
+// stores fill whole sectors.  Four block barriers per span with new vertices,
+// one per span without.
 constexpr int kLgUnroll = 8;
 constexpr int kLgMinBlocks = 3;  // 768 threads per SM: at most 80 registers
 
@@ -904,7 +906,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     // pass 1: indptr pairs (and original ids, for parents) into shared
     // memory; per-lane kept-entry count, degree and chunk sums.  Every
     // round's loads are issued before the first use.
-    uint32_t n_cnt = 0, n_deg = 0, n_chk = 0;
+    uint32_t n_cnt = 0, n_deg = 0, n_chk = 0;  // n_cnt: kept so far (warp-uniform)
     for (uint32_t t0 = lo; t0 < hi; t0 += 32u * kLgUnroll) {
       uint32_t b[kLgUnroll], e[kLgUnroll], o[kLgUnroll];
 #pragma unroll
@@ -922,21 +924,24 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
           }
         }
       }
+      // kept entries (degree > 0) compacted in place, in list order: entry
+      // positions only move down, and this iteration's entries are already
+      // in registers
 #pragma unroll
       for (int r = 0; r < kLgUnroll; r++) {
-        const uint32_t i = t0 + 32u * r + lane;
-        const uint32_t deg = e[r] - b[r];
-        if (i < hi) {
-          if (PAR) s_o[i] = o[r];
-          s_b[i] = b[r];
-          s_d[i] = deg;
+        const uint32_t deg = e[r] - b[r];  // 0 past hi
+        const uint32_t km = __ballot_sync(kFull, deg > 0u);
+        if (deg) {
+          const uint32_t p = lo + n_cnt + __popc(km & lt_mask);
+          s_b[p] = b[r];
+          s_d[p] = deg;
+          if (PAR) s_o[p] = o[r];
         }
-        n_cnt += deg > 0u;
+        n_cnt += __popc(km);
         n_deg += deg;
         n_chk += edge_chunks(b[r], deg, off);
       }
     }
-    n_cnt = __reduce_add_sync(kFull, n_cnt);
     n_deg = __reduce_add_sync(kFull, n_deg);
     n_chk = __reduce_add_sync(kFull, n_chk);
     if (lane == 0) {
@@ -958,28 +963,35 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     }
     __syncthreads();
     if (n_cnt) {
-      // pass 2: the kept entries, in list order
+      // pass 2: the kept entries in 32-slot windows aligned to 128 bytes,
+      // two windows per step (their scans overlap)
       const unsigned long long wb = s_base + s_wtot[warp];
-      uint32_t slot = (uint32_t)(wb >> 32), prefc = (uint32_t)wb;
-      for (uint32_t t0 = lo; t0 < hi; t0 += 32u) {
-        const uint32_t i = t0 + lane;
-        uint32_t b = 0, deg = 0;
-        if (i < hi) {
-          b = s_b[i];
-          deg = s_d[i];
+      const uint32_t slot0 = (uint32_t)(wb >> 32), end = slot0 + n_cnt;
+      uint32_t prefc = (uint32_t)wb;
+      for (uint32_t ws = slot0 & ~31u; ws < end; ws += 64u) {
+        uint32_t b[2], deg[2], nch[2], cincl[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const uint32_t sl = ws + 32u * h + lane;
+          b[h] = deg[h] = 0;
+          if (sl >= slot0 && sl < end) {
+            b[h] = s_b[lo + (sl - slot0)];
+            deg[h] = s_d[lo + (sl - slot0)];
+          }
+          nch[h] = edge_chunks(b[h], deg[h], off);
+          cincl[h] = warp_incl_scan(nch[h], lane);
         }
-        const uint32_t nch = edge_chunks(b, deg, off);
-        const uint32_t km = __ballot_sync(kFull, deg > 0u);
-        const uint32_t cincl = warp_incl_scan(nch, lane);
-        if (deg) {
-          const uint32_t sl = slot + __popc(km & lt_mask);
-          qb[sl] = b;
-          qd[sl] = deg;
-          qc[sl] = prefc + cincl - nch;
-          if (PAR) qv[sl] = s_o[i];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const uint32_t sl = ws + 32u * h + lane;
+          if (deg[h]) {  // exactly the slots in [slot0, end)
+            qb[sl] = b[h];
+            qd[sl] = deg[h];
+            qc[sl] = prefc + cincl[h] - nch[h];
+            if (PAR) qv[sl] = s_o[lo + (sl - slot0)];
+          }
+          prefc += __shfl_sync(kFull, cincl[h], 31);
         }
-        slot += __popc(km);
-        prefc += __shfl_sync(kFull, cincl, 31);
       }
     }
     // the list is rewritten only after the next span's first barrier, so

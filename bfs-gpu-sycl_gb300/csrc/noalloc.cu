@@ -8,7 +8,7 @@
 // memory it already owns), and the BFS workspace -- visited bitmaps, the two
 // frontier queues and the level-loop state -- lives in the file-scope device
 // array below.  It is sized for graphs of at most BFS_NOALLOC_MAX_VERTICES
-// vertices (about 32 MiB), and every GPU that loads this library keeps it
+// vertices (about 33 MiB), and every GPU that loads this library keeps it
 // until the process exits.
 //
 // Set-up: the first call on a device, with that device current, looks up the

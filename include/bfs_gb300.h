@@ -275,7 +275,7 @@ int32_t bfs_multi_num_configs(int32_t *blocks, int32_t *ipts, int32_t *clusters,
  * One BFS from root over a CSC graph already on the current device, into
  * levels_dev (n_cols int32, caller-owned); *edges_count_out (optional, host)
  * receives the reference's edgesCount.  The workspace is a fixed device array
- * inside the library (about 32 MiB per GPU that loads it, held until exit),
+ * inside the library (about 33 MiB per GPU that loads it, held until exit),
  * so graphs are limited to BFS_NOALLOC_MAX_VERTICES vertices and larger ones
  * are rejected with BFS_ERR_INVALID_ARG.  The first call on a device looks
  * up that array's address (make it before any stream capture), and under

@@ -485,7 +485,7 @@ def run_gb300(a):
     # model's choice from the level's features, against the per-level best
     regret = None
     if weights is not None and not a.skip_arms:
-        t_sel, t_best, t_llb, per_level = 0.0, 0.0, 0.0, []
+        t_sel, t_best, per_level = 0.0, 0.0, []
         for r in roots[a.warmup:a.warmup + 2]:
             smp = dg.sched_record(int(r), reps=2)
             feats = np.array([list(x.features) for x in smp], np.float32)
@@ -495,11 +495,9 @@ def run_gb300(a):
                 best = ms[i].min()
                 t_sel += ms[i][chosen[i]]
                 t_best += best
-                t_llb += ms[i][1]
                 per_level.append(round(float(ms[i][chosen[i]] / best - 1.0), 4) if best > 0 else 0.0)
         regret = {"explore_regret_frac": round(t_sel / t_best - 1.0, 4),
                   "per_level_regret": per_level,
-                  "explore_speedup_vs_llb256": round(t_llb / t_sel, 3),
                   "roots": 2, "levels": len(per_level),
                   "method": "bfs_sched_record: every level timed with all 9 explore arms from the "
                             "same state (best of 2); regret = time of the model's arm / best arm - 1"}

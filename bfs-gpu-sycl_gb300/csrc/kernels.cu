@@ -756,28 +756,37 @@ __device__ __forceinline__ uint32_t merge_levels(uint32_t word, uint32_t bits, u
   return (word & ~m) | (rep & m);
 }
 
-// Level generation.  Blocks claim spans of B bitmap words (one word per
-// thread) from a counter -- the density of new vertices is uneven over the
-// bitmap.  A block takes the claim of its next span when the current one
-// starts and loads the next span's words while it works on the current one.
-// Each thread writes its word's new levels into the working levels: the
-// word's 32 vertices are one 32-byte sector there, read when the word is
-// seen and written back whole once the block's list is built.  The block
-// lists the span's new vertices (vis & ~prev) in shared memory in vertex
-// order (a block scan of the words' popcounts; each thread walks its word's
-// set bits), then every warp takes an equal share of the list, whatever the
-// bit layout.  Pass 1 loads each entry's indptr pair (kLgUnroll rounds of
-// loads in flight per lane), keeps the entry's offset and degree in shared
-// memory in place of it, and counts kept entries, their degrees and their
-// 16-byte chunks; thread 0 reserves the block's queue slots and chunk
-// offsets with one atomic -- slots and the chunk prefix must come from the
-// same atomic, so that the prefix is in slot order -- and adds the degrees to
-// the level's edge total; pass 2 compacts the kept entries in shared memory
-// and writes them in 32-slot windows aligned to 128 bytes, so that the queue
-// stores fill whole sectors.  Four block barriers per span with new vertices,
-// one per span without.
+// Level generation.  After a level that explored many edges, blocks claim
+// spans of B bitmap words (one word per thread) from a counter -- the
+// density of new vertices is uneven over the bitmap -- and load each span's
+// words while working on the previous one.  The thread owning a word merges
+// its new vertices' levels into the working levels: the word's 32 vertices
+// are one 32-byte sector there, read when the word is seen and written back
+// whole once the block's list is built.  The block lists the span's new
+// vertices (vis & ~prev) in shared memory in vertex order (a block scan of
+// the words' popcounts; each thread walks its word's set bits), then every
+// warp takes an equal share of the list, whatever the bit layout.  Pass 1
+// loads each entry's indptr pair (kLgUnroll rounds of loads in flight per
+// lane), compacts the kept entries in place with their offset and degree,
+// and counts them, their degrees and their 16-byte chunks; thread 0 reserves
+// the block's queue slots and chunk offsets with one atomic -- slots and the
+// chunk prefix must come from the same atomic, so that the prefix is in slot
+// order -- and adds the degrees to the level's edge total; pass 2 writes the
+// kept entries in 32-slot windows aligned to 128 bytes, so that the queue
+// stores fill whole sectors.  Four block barriers per span with new
+// vertices, one per span without.
+//
+// After a level that explored fewer than words / 8 edges (at most that many
+// words hold new vertices, and on graphs of large diameter they are spread
+// thinly over every span) the warps work on their own, without block
+// barriers: warp g of the grid takes the 32-word groups g, g + G, g + 2G, ...
+// (G warps), four groups' words in flight at a time, lists the new vertices
+// in its own slice of the list and runs pass 1, one queue reservation and
+// pass 2 on the slice when the next group's entries would not fit in it, and
+// at the end.
 constexpr int kLgUnroll = 8;
 constexpr int kLgMinBlocks = 3;  // 768 threads per SM: at most 80 registers
+constexpr int kLgSparseGroups = 4;  // 32-word groups per warp step (sparse levels)
 
 template <int B, bool PAR>
 __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *__restrict__ st,
@@ -786,7 +795,9 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   constexpr int NW = B / 32;
   constexpr uint32_t kSpan = B;         // words per block and step
   constexpr uint32_t kCap = kSpan * 32u;  // list capacity: every vertex of a span
+  constexpr uint32_t kSlice = kCap / NW;  // a warp's slice: every vertex of 32 words
   static_assert((NW & (NW - 1)) == 0, "warps per block: a power of two");
+  static_assert(kSlice == 1024u, "a warp's slice holds 32 words' vertices");
   static_assert(kSchedParams <= kCap, "the model must fit the list buffer");
   // list: entry (vertex id, bit 31 the moved flag), then its indptr offset;
   // degrees; original ids (parents only)
@@ -797,6 +808,7 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   __shared__ uint32_t s_wc[2][NW];
   __shared__ unsigned long long s_wtot[NW];
   __shared__ uint32_t s_wdeg[NW];
+  __shared__ uint32_t s_wreach[NW];
   __shared__ unsigned long long s_base;
   __shared__ uint32_t s_sb[2];
   __shared__ int s_last;
@@ -823,90 +835,42 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
   const uint32_t id_mask = moved ? 0x7FFFFFFFu : 0xFFFFFFFFu;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t reached = 0;  // thread 0's count of the block's new vertices
+  const uint32_t rep = (lvl_next < (int32_t)kLv8Deep ? (uint32_t)lvl_next : kLv8Deep) *
+                       0x01010101u;  // the new level in every byte
+  // new vertices and kept entries' degrees counted by this lane (summed over
+  // the block at the end)
+  uint32_t my_reached = 0, my_deg = 0;
 
-  if (threadIdx.x == 0) s_sb[0] = atomicAdd(&st->lg_cursor, kSpan);
-  __syncthreads();
-  uint32_t sb = s_sb[0];
-  // this thread's word of the current span: vis, prev, moved
-  uint32_t vw = 0, pw = 0, mw = 0;
-  if (sb + threadIdx.x < words) {
-    vw = V[sb + threadIdx.x];
-    pw = P[sb + threadIdx.x];
-    if (moved) mw = moved[sb + threadIdx.x];
-  }
-  for (uint32_t step = 0; sb < words; step ^= 1u) {
-    const uint32_t w = sb + threadIdx.x;
-    uint32_t x = vw & ~pw;
-    const uint32_t xn = x, xm = mw;
-    // the word's working levels, merged and written back after the list
+  // the working levels of word w with new bits x: sector (l0, l1) merged and
+  // written back; a deep level also goes to the output (original ids)
+  auto write_levels = [&](uint32_t w, uint32_t x, uint32_t xm, uint4 l0, uint4 l1) {
     uint4 *__restrict__ sec = reinterpret_cast<uint4 *>(lv8) + 2u * (size_t)w;
-    uint4 l0 = make_uint4(0u, 0u, 0u, 0u), l1 = l0;
-    if (x) {  // x != 0 only for words < words
-      P[w] = vw;
-      l0 = sec[0];
-      l1 = sec[1];
-    }
-    const uint32_t c = __popc(x);
-    const uint32_t incl = warp_incl_scan(c, lane);
-    if (lane == 31) s_wc[step][warp] = incl;
-    if (threadIdx.x == 0) s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
-    __syncthreads();
-    uint32_t L = 0, woff = 0;
-#pragma unroll
-    for (int i = 0; i < NW; i++) {
-      const uint32_t y = s_wc[step][i];
-      woff += (uint32_t)i < warp ? y : 0u;
-      L += y;
-    }
-    // the next span's words, in flight while this span is worked on
-    sb = s_sb[step ^ 1u];
-    vw = pw = mw = 0;
-    if (sb + threadIdx.x < words) {
-      vw = V[sb + threadIdx.x];
-      pw = P[sb + threadIdx.x];
-      if (moved) mw = moved[sb + threadIdx.x];
-    }
-    if (L == 0) continue;  // uniform over the block
-    reached += L;
-    {
-      uint32_t pos = woff + incl - c;
-      const uint32_t vbase = w * 32u;
-      while (x) {
-        const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
-        s_b[pos++] = (vbase + bpos) | (((xm >> bpos) & 1u) << 31);
-        x &= x - 1u;
+    l0.x = merge_levels(l0.x, x, rep);
+    l0.y = merge_levels(l0.y, x >> 4, rep);
+    l0.z = merge_levels(l0.z, x >> 8, rep);
+    l0.w = merge_levels(l0.w, x >> 12, rep);
+    l1.x = merge_levels(l1.x, x >> 16, rep);
+    l1.y = merge_levels(l1.y, x >> 20, rep);
+    l1.z = merge_levels(l1.z, x >> 24, rep);
+    l1.w = merge_levels(l1.w, x >> 28, rep);
+    sec[0] = l0;
+    sec[1] = l1;
+    if (lvl_next >= (int32_t)kLv8Deep) {
+      for (uint32_t y = x; y; y &= y - 1u) {
+        const uint32_t bpos = (uint32_t)(__ffs(y) - 1);
+        const uint32_t v = w * 32u + bpos;
+        level[((xm >> bpos) & 1u) ? perm[v] : v] = lvl_next;
       }
     }
-    if (xn) {
-      const uint32_t rep = (lvl_next < (int32_t)kLv8Deep ? (uint32_t)lvl_next : kLv8Deep) *
-                           0x01010101u;
-      l0.x = merge_levels(l0.x, xn, rep);
-      l0.y = merge_levels(l0.y, xn >> 4, rep);
-      l0.z = merge_levels(l0.z, xn >> 8, rep);
-      l0.w = merge_levels(l0.w, xn >> 12, rep);
-      l1.x = merge_levels(l1.x, xn >> 16, rep);
-      l1.y = merge_levels(l1.y, xn >> 20, rep);
-      l1.z = merge_levels(l1.z, xn >> 24, rep);
-      l1.w = merge_levels(l1.w, xn >> 28, rep);
-      sec[0] = l0;
-      sec[1] = l1;
-      if (lvl_next >= (int32_t)kLv8Deep) {
-        // deep level: the level itself goes to the output (original ids)
-        for (uint32_t y = xn; y; y &= y - 1u) {
-          const uint32_t bpos = (uint32_t)(__ffs(y) - 1);
-          const uint32_t v = w * 32u + bpos;
-          level[((xm >> bpos) & 1u) ? perm[v] : v] = lvl_next;
-        }
-      }
-    }
-    __syncthreads();
-    // this warp's share of the list
-    const uint32_t lo = (L * warp) / NW, hi = (L * (warp + 1u)) / NW;
-    // pass 1: indptr pairs (and original ids, for parents) into shared
-    // memory; per-lane kept-entry count, degree and chunk sums.  Every
-    // round's loads are issued before the first use.
-    uint32_t n_cnt = 0, n_deg = 0, n_chk = 0;  // n_cnt: kept so far (warp-uniform)
+  };
+  // Pass 1 over list entries [lo, hi) (one warp): every round's loads are
+  // issued before their first use; kept entries (degree > 0) are compacted
+  // in place, in list order, to [lo, lo + count) -- positions only move down
+  // and an iteration's entries are already in registers.  Returns the warp's
+  // kept count, degree and chunk sums (uniform over the warp).
+  auto pass1 = [&](uint32_t lo, uint32_t hi, uint32_t &n_cnt, uint32_t &n_deg,
+                   uint32_t &n_chk) {
+    n_cnt = n_deg = n_chk = 0;
     for (uint32_t t0 = lo; t0 < hi; t0 += 32u * kLgUnroll) {
       uint32_t b[kLgUnroll], e[kLgUnroll], o[kLgUnroll];
 #pragma unroll
@@ -924,9 +888,6 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
           }
         }
       }
-      // kept entries (degree > 0) compacted in place, in list order: entry
-      // positions only move down, and this iteration's entries are already
-      // in registers
 #pragma unroll
       for (int r = 0; r < kLgUnroll; r++) {
         const uint32_t deg = e[r] - b[r];  // 0 past hi
@@ -944,69 +905,204 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
     }
     n_deg = __reduce_add_sync(kFull, n_deg);
     n_chk = __reduce_add_sync(kFull, n_chk);
-    if (lane == 0) {
-      s_wtot[warp] = ((unsigned long long)n_cnt << 32) | n_chk;
-      s_wdeg[warp] = n_deg;
+  };
+  // Pass 2 (one warp): the n_cnt kept entries at [lo, lo + n_cnt) to queue
+  // slots from wb (slot << 32 | chunk offset), in 32-slot windows aligned to
+  // 128 bytes, two windows per step (their scans overlap).
+  auto pass2 = [&](uint32_t lo, uint32_t n_cnt, unsigned long long wb) {
+    const uint32_t slot0 = (uint32_t)(wb >> 32), end = slot0 + n_cnt;
+    uint32_t prefc = (uint32_t)wb;
+    for (uint32_t ws = slot0 & ~31u; ws < end; ws += 64u) {
+      uint32_t b[2], deg[2], nch[2], cincl[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t sl = ws + 32u * h + lane;
+        b[h] = deg[h] = 0;
+        if (sl >= slot0 && sl < end) {
+          b[h] = s_b[lo + (sl - slot0)];
+          deg[h] = s_d[lo + (sl - slot0)];
+        }
+        nch[h] = edge_chunks(b[h], deg[h], off);
+        cincl[h] = warp_incl_scan(nch[h], lane);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t sl = ws + 32u * h + lane;
+        if (deg[h]) {  // exactly the slots in [slot0, end)
+          qb[sl] = b[h];
+          qd[sl] = deg[h];
+          qc[sl] = prefc + cincl[h] - nch[h];
+          if (PAR) qv[sl] = s_o[lo + (sl - slot0)];
+        }
+        prefc += __shfl_sync(kFull, cincl[h], 31);
+      }
     }
+  };
+
+  if (st->EF >= (words >> 3)) {  // uniform over the grid: the block path
+    if (threadIdx.x == 0) s_sb[0] = atomicAdd(&st->lg_cursor, kSpan);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned long long run = 0;
-      uint32_t deg_sum = 0;
+    uint32_t sb = s_sb[0];
+    // this thread's word of the current span: vis, prev, moved
+    uint32_t vw = 0, pw = 0, mw = 0;
+    if (sb + threadIdx.x < words) {
+      vw = V[sb + threadIdx.x];
+      pw = P[sb + threadIdx.x];
+      if (moved) mw = moved[sb + threadIdx.x];
+    }
+    for (uint32_t step = 0; sb < words; step ^= 1u) {
+      const uint32_t w = sb + threadIdx.x;
+      uint32_t x = vw & ~pw;
+      const uint32_t xn = x, xm = mw;
+      // the word's working levels, merged and written back after the list
+      uint4 l0 = make_uint4(0u, 0u, 0u, 0u), l1 = l0;
+      if (x) {  // x != 0 only for words < words
+        P[w] = vw;
+        const uint4 *sec = reinterpret_cast<const uint4 *>(lv8) + 2u * (size_t)w;
+        l0 = sec[0];
+        l1 = sec[1];
+      }
+      const uint32_t c = __popc(x);
+      const uint32_t incl = warp_incl_scan(c, lane);
+      if (lane == 31) s_wc[step][warp] = incl;
+      if (threadIdx.x == 0) s_sb[step ^ 1u] = atomicAdd(&st->lg_cursor, kSpan);
+      __syncthreads();
+      uint32_t L = 0, woff = 0;
+#pragma unroll
       for (int i = 0; i < NW; i++) {
-        const unsigned long long y = s_wtot[i];
-        s_wtot[i] = run;
-        run += y;
-        deg_sum += s_wdeg[i];
+        const uint32_t y = s_wc[step][i];
+        woff += (uint32_t)i < warp ? y : 0u;
+        L += y;
       }
-      s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
-      if (deg_sum) atomicAdd(&st->next_edges, deg_sum);  // a total: order does not matter
-    }
-    __syncthreads();
-    if (n_cnt) {
-      // pass 2: the kept entries in 32-slot windows aligned to 128 bytes,
-      // two windows per step (their scans overlap)
-      const unsigned long long wb = s_base + s_wtot[warp];
-      const uint32_t slot0 = (uint32_t)(wb >> 32), end = slot0 + n_cnt;
-      uint32_t prefc = (uint32_t)wb;
-      for (uint32_t ws = slot0 & ~31u; ws < end; ws += 64u) {
-        uint32_t b[2], deg[2], nch[2], cincl[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const uint32_t sl = ws + 32u * h + lane;
-          b[h] = deg[h] = 0;
-          if (sl >= slot0 && sl < end) {
-            b[h] = s_b[lo + (sl - slot0)];
-            deg[h] = s_d[lo + (sl - slot0)];
-          }
-          nch[h] = edge_chunks(b[h], deg[h], off);
-          cincl[h] = warp_incl_scan(nch[h], lane);
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const uint32_t sl = ws + 32u * h + lane;
-          if (deg[h]) {  // exactly the slots in [slot0, end)
-            qb[sl] = b[h];
-            qd[sl] = deg[h];
-            qc[sl] = prefc + cincl[h] - nch[h];
-            if (PAR) qv[sl] = s_o[lo + (sl - slot0)];
-          }
-          prefc += __shfl_sync(kFull, cincl[h], 31);
+      // the next span's words, in flight while this span is worked on
+      sb = s_sb[step ^ 1u];
+      vw = pw = mw = 0;
+      if (sb + threadIdx.x < words) {
+        vw = V[sb + threadIdx.x];
+        pw = P[sb + threadIdx.x];
+        if (moved) mw = moved[sb + threadIdx.x];
+      }
+      if (L == 0) continue;  // uniform over the block
+      if (threadIdx.x == 0) my_reached += L;
+      {
+        uint32_t pos = woff + incl - c;
+        const uint32_t vbase = w * 32u;
+        while (x) {
+          const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
+          s_b[pos++] = (vbase + bpos) | (((xm >> bpos) & 1u) << 31);
+          x &= x - 1u;
         }
       }
+      if (xn) write_levels(w, xn, xm, l0, l1);
+      __syncthreads();
+      // this warp's share of the list
+      const uint32_t lo = (L * warp) / NW, hi = (L * (warp + 1u)) / NW;
+      uint32_t n_cnt, n_deg, n_chk;
+      pass1(lo, hi, n_cnt, n_deg, n_chk);
+      if (lane == 0) {
+        s_wtot[warp] = ((unsigned long long)n_cnt << 32) | n_chk;
+        s_wdeg[warp] = n_deg;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int i = 0; i < NW; i++) {
+          const unsigned long long y = s_wtot[i];
+          s_wtot[i] = run;
+          run += y;
+          my_deg += s_wdeg[i];
+        }
+        s_base = run ? atomicAdd(&st->next_packed, run) : 0ull;
+      }
+      __syncthreads();
+      if (n_cnt) pass2(lo, n_cnt, s_base + s_wtot[warp]);
+      // the list is rewritten only after the next span's first barrier, so
+      // pass 2 needs no trailing barrier
     }
-    // the list is rewritten only after the next span's first barrier, so
-    // pass 2 needs no trailing barrier
+  } else {  // the warp path (sparse levels)
+    const uint32_t groups = words >> 5;  // words is a multiple of 32
+    const uint32_t gwarp = blockIdx.x * NW + warp, nwarps = gridDim.x * NW;
+    const uint32_t lo = warp * kSlice;  // this warp's slice of the list
+    uint32_t size = 0;                  // entries in the slice
+    auto flush = [&]() {
+      uint32_t n_cnt, n_deg, n_chk;
+      pass1(lo, lo + size, n_cnt, n_deg, n_chk);
+      if (n_cnt) {
+        unsigned long long wb = 0;
+        if (lane == 0) {
+          wb = atomicAdd(&st->next_packed, ((unsigned long long)n_cnt << 32) | n_chk);
+          my_deg += n_deg;
+        }
+        pass2(lo, n_cnt, __shfl_sync(kFull, wb, 0));
+      }
+      size = 0;
+      __syncwarp();  // pass 2's reads of the slice are done
+    };
+    for (uint32_t g0 = gwarp; g0 < groups; g0 += kLgSparseGroups * nwarps) {
+      uint32_t vw[kLgSparseGroups], pw[kLgSparseGroups], mw[kLgSparseGroups];
+#pragma unroll
+      for (int k = 0; k < kLgSparseGroups; k++) {
+        const uint32_t g = g0 + k * nwarps;
+        vw[k] = pw[k] = mw[k] = 0;
+        if (g < groups) {
+          vw[k] = V[g * 32u + lane];
+          pw[k] = P[g * 32u + lane];
+          if (moved) mw[k] = moved[g * 32u + lane];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kLgSparseGroups; k++) {
+        uint32_t x = vw[k] & ~pw[k];
+        if (!__any_sync(kFull, x != 0u)) continue;  // uniform over the warp
+        const uint32_t w = (g0 + k * nwarps) * 32u + lane;
+        uint4 l0 = make_uint4(0u, 0u, 0u, 0u), l1 = l0;
+        if (x) {
+          P[w] = vw[k];
+          const uint4 *sec = reinterpret_cast<const uint4 *>(lv8) + 2u * (size_t)w;
+          l0 = sec[0];
+          l1 = sec[1];
+        }
+        const uint32_t c = __popc(x);
+        const uint32_t incl = warp_incl_scan(c, lane);
+        const uint32_t tot = __shfl_sync(kFull, incl, 31);
+        my_reached += c;
+        if (size + tot > kSlice) flush();
+        uint32_t pos = lo + size + incl - c;
+        const uint32_t vbase = w * 32u, xn = x;
+        while (x) {
+          const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
+          s_b[pos++] = (vbase + bpos) | (((mw[k] >> bpos) & 1u) << 31);
+          x &= x - 1u;
+        }
+        if (xn) write_levels(w, xn, mw[k], l0, l1);
+        size += tot;
+        __syncwarp();  // the slice's entries are written
+      }
+    }
+    if (size) flush();
   }
 
-  // fused scheduler (learned runs): every block copies the model into its
-  // (now unused) list buffer while thread 0 takes the block's ticket, so
-  // that the last block -- which picks the next level's arm -- holds it by
+  // Block totals, then the ticket.  Learned runs: every block copies the
+  // model into its (now unused) list buffer while thread 0 takes the ticket,
+  // so that the last block -- which picks the next level's arm -- holds it by
   // the time it knows it is last.  Thread 0 stays out of the copy: its fence
   // would otherwise wait for its share of the loads.
+  my_reached = __reduce_add_sync(kFull, my_reached);
+  if (lane == 0) {
+    s_wreach[warp] = my_reached;
+    s_wdeg[warp] = my_deg;
+  }
+  __syncthreads();  // also: every warp is done with the list
   const float *w = st->sched_w;
   float *s_w = reinterpret_cast<float *>(s_dyn);
-  if (w != nullptr) __syncthreads();
   if (threadIdx.x == 0) {
+    uint32_t reached = 0, deg_sum = 0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) {
+      reached += s_wreach[i];
+      deg_sum += s_wdeg[i];
+    }
+    if (deg_sum) atomicAdd(&st->next_edges, deg_sum);  // a total: order does not matter
     if (reached) atomicAdd(&st->reached, reached);
     __threadfence();
     const uint32_t ticket = atomicAdd(&st->done_blocks, 1u);

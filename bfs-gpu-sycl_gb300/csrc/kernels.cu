@@ -780,10 +780,10 @@ __device__ __forceinline__ uint32_t merge_levels(uint32_t word, uint32_t bits, u
 // words hold new vertices, and on graphs of large diameter they are spread
 // thinly over every span) the warps work on their own, without block
 // barriers: warp g of the grid takes the 32-word groups g, g + G, g + 2G, ...
-// (G warps), four groups' words in flight at a time, lists the new vertices
-// in its own slice of the list and runs pass 1, one queue reservation and
-// pass 2 on the slice when the next group's entries would not fit in it, and
-// at the end.
+// (G warps), four groups' words in flight at a time, writes the new
+// vertices' working levels as single bytes, lists them in its own slice of
+// the list and runs pass 1, one queue reservation and pass 2 on the slice
+// when the next group's entries would not fit in it, and at the end.
 constexpr int kLgUnroll = 8;
 constexpr int kLgMinBlocks = 3;  // 768 threads per SM: at most 80 registers
 constexpr int kLgSparseGroups = 4;  // 32-word groups per warp step (sparse levels)
@@ -1055,26 +1055,27 @@ __global__ void __launch_bounds__(B, kLgMinBlocks) levelgen_kernel(BfsDevState *
         uint32_t x = vw[k] & ~pw[k];
         if (!__any_sync(kFull, x != 0u)) continue;  // uniform over the warp
         const uint32_t w = (g0 + k * nwarps) * 32u + lane;
-        uint4 l0 = make_uint4(0u, 0u, 0u, 0u), l1 = l0;
-        if (x) {
-          P[w] = vw[k];
-          const uint4 *sec = reinterpret_cast<const uint4 *>(lv8) + 2u * (size_t)w;
-          l0 = sec[0];
-          l1 = sec[1];
-        }
+        if (x) P[w] = vw[k];
         const uint32_t c = __popc(x);
         const uint32_t incl = warp_incl_scan(c, lane);
         const uint32_t tot = __shfl_sync(kFull, incl, 31);
         my_reached += c;
         if (size + tot > kSlice) flush();
         uint32_t pos = lo + size + incl - c;
-        const uint32_t vbase = w * 32u, xn = x;
+        const uint32_t vbase = w * 32u;
+        // few new vertices per word here: their working levels are single
+        // byte stores (the array is in L2), with no read of the sector
         while (x) {
           const uint32_t bpos = (uint32_t)(__ffs(x) - 1);
-          s_b[pos++] = (vbase + bpos) | (((mw[k] >> bpos) & 1u) << 31);
+          const uint32_t mv = (mw[k] >> bpos) & 1u;
+          s_b[pos++] = (vbase + bpos) | (mv << 31);
+          lv8[vbase + bpos] = (uint8_t)rep;
+          if (lvl_next >= (int32_t)kLv8Deep) {
+            const uint32_t v = vbase + bpos;
+            level[mv ? perm[v] : v] = lvl_next;
+          }
           x &= x - 1u;
         }
-        if (xn) write_levels(w, xn, mw[k], l0, l1);
         size += tot;
         __syncwarp();  // the slice's entries are written
       }

@@ -24,13 +24,14 @@
 //             levels) at a time, and list each span's new vertices in shared
 //             memory; warps take equal shares of the list and load degrees
 //             32 at a time, and one atomic per block and span reserves the
-//             queue tail.  The atomic adds (count << 32 | chunk count), so
-//             every entry also receives the exclusive prefix of its 16-byte
-//             edge chunks in queue order: the grid-wide scan that GLB needs
-//             comes out of the same atomic.  Zero-degree vertices and
-//             vertices >= n_rows get their level but are not queued (they
-//             would expand nothing; run_bfs_cpu.hpp:31 never expands
-//             tid >= numRows).
+//             queue tail (after levels with few edges, warps do the same on
+//             their own, without block barriers).  The atomic adds
+//             (count << 32 | chunk count), so every entry also receives the
+//             exclusive prefix of its 16-byte edge chunks in queue order: the
+//             grid-wide scan that GLB needs comes out of the same atomic.
+//             Zero-degree vertices and vertices >= n_rows get their level
+//             but are not queued (they would expand nothing;
+//             run_bfs_cpu.hpp:31 never expands tid >= numRows).
 //   finish    the last level-generation block swaps the queues, accumulates
 //             edgesCount and, in the CUDA-graph loop, sets the while-node
 //             condition, so no host round trip happens between levels.

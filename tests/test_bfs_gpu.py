@@ -334,3 +334,38 @@ def test_run_roots_pinned_and_pageable(B, O):
         dg.run_roots([roots[0], n, roots[1]], [a.ctypes.data for a in bad])
     assert all(np.all(a == 7) for a in bad)
     dg.free()
+
+
+def test_sparse_level_generation_slice_overflow(B, O):
+    """After a level with few edges, level generation runs per warp: warp g
+    takes the 32-word groups g, g + G, g + 2G, ... (G warps: 3 blocks of 8 per
+    SM) into a 1024-entry slice and flushes it when the next group would not
+    fit.  A root whose 2048 out-edges fill groups 0 and G (every vertex new,
+    2048 edges < words / 8) makes warp 0 flush between its groups; levels and
+    edge counts stay exact, in both loops and every arm."""
+    torch = torch_cuda()
+    G = torch.cuda.get_device_properties(0).multi_processor_count * 3 * 8
+    n = max((G + 1) * 1024 * 4, 1 << 22)
+    targets = np.concatenate([np.arange(0, 1024), np.arange(G * 1024, G * 1024 + 1024)])
+    root = n - 1
+    # root -> targets; every target -> root + a second hop to a fresh vertex
+    second = (targets + 2 * G * 1024 + 5) % (n - 1)
+    src = np.concatenate([np.full(len(targets), root), targets, targets])
+    dst = np.concatenate([targets, np.full(len(targets), root), second])
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    keep = np.ones(len(src), bool)
+    keep[1:] = (src[1:] != src[:-1]) | (dst[1:] != dst[:-1])
+    src, dst = src[keep], dst[keep]
+    indptr = np.zeros(n + 1, np.uint32)
+    indptr[1:] = np.cumsum(np.bincount(src, minlength=n))
+    g = B.Csc(indptr, dst.astype(np.uint32))
+    dg = B.Graph.upload(g)
+    ref, ec = O.oracle_bfs(g.indptr, g.inds, root)
+    assert (ref == 1).sum() == 2048
+    for lb, blk in (("llb", 256), ("glb", 256), ("slb", 128), ("learned", 256)):
+        for loop in ("graph", "host"):
+            lv, _, st = dg.run(root, B.options(lb, blk, loop=loop))
+            assert np.array_equal(lv, ref), (lb, loop)
+            assert st.edges_count == ec
+    dg.free()

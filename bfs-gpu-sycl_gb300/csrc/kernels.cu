@@ -772,10 +772,10 @@ __device__ __forceinline__ uint32_t merge_levels(uint32_t word, uint32_t bits, u
 // and counts them, their degrees and their 16-byte chunks; thread 0 reserves
 // the block's queue slots and chunk offsets with one atomic -- slots and the
 // chunk prefix must come from the same atomic, so that the prefix is in slot
-// order -- and adds the degrees to the level's edge total; pass 2 writes the
-// kept entries in 32-slot windows aligned to 128 bytes, so that the queue
-// stores fill whole sectors.  Four block barriers per span with new
-// vertices, one per span without.
+// order; pass 2 writes the kept entries in 32-slot windows aligned to 128
+// bytes, so that the queue stores fill whole sectors.  Four block barriers
+// per span with new vertices, one per span without.  Degree and vertex
+// totals go to the level's counters once per block, at the end.
 //
 // After a level that explored fewer than words / 8 edges (at most that many
 // words hold new vertices, and on graphs of large diameter they are spread

@@ -14,6 +14,10 @@ sees a known sequence of launches:
                   the block size, e.g. glb256.  HUB: the hub layout's prefix
                   size (0 = off; default: automatic).  Prints (level,
                   frontier entries, edges) per level.
+  grid SIDE ARM   SIDE x SIDE 4-neighbour grid with 5 % of edges deleted (seed
+                  3), one BFS from the first seeded root, host-driven level
+                  loop, as above: thousands of small levels (level generation
+                  takes its warp path after each).
   batch SCALE     R-MAT SCALE/EF16 seed 6, one 64-root multi-source pass
                   (host-driven level loop, as above).
   multi [B I C]   the 256-graph mixed batch of the benchmark, one launch of
@@ -48,6 +52,14 @@ def case_bfs(scale, arm, hub=-1):
     print("ms", st.device_ms, "edges", st.edges_count)
 
 
+def case_grid(side, arm):
+    dg = B.Graph.upload(B.gen_grid(side, side, 0.05, 3), validate=False)
+    r = int(B.sample_roots(dg.download(), 1, 3)[0])
+    lv = torch.empty(dg.n_cols, dtype=torch.int32, device="cuda")
+    st = dg.run_device(r, lv.data_ptr(), opts=B.options(arm[:3], int(arm[3:]), loop="host"))
+    print("levels", st.num_levels, "ms", st.device_ms, "edges", st.edges_count)
+
+
 def case_batch(scale):
     dg = B.Graph.gen_rmat_device(scale, 16, seed=6)
     roots = B.sample_roots(dg.download(), 64, 6)
@@ -72,6 +84,8 @@ def main(argv):
     torch.cuda.set_device(0)
     if argv[0] == "bfs" and len(argv) in (3, 4):
         case_bfs(int(argv[1]), argv[2], *(int(x) for x in argv[3:]))
+    elif argv[0] == "grid" and len(argv) == 3:
+        case_grid(int(argv[1]), argv[2])
     elif argv[0] == "batch" and len(argv) == 2:
         case_batch(int(argv[1]))
     elif argv[0] == "multi" and len(argv) in (1, 4):
